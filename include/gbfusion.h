@@ -1,0 +1,256 @@
+/*
+ * gbfusion.h -- C ABI of libgbfusion, the GB300 (sm_103a) dense RGB-D fusion
+ * hot path: voxel-hashed TSDF mapping (allocation, visible-block enumeration,
+ * integration, raycast, marching cubes) and point-to-plane ICP + photometric
+ * tracking over image pyramids.
+ *
+ * Every entry point returns a gbf_status; on failure gbf_last_error() gives a
+ * message (thread-local).  No entry point exits the process (the reference's
+ * safe_call does exit(0), include/utils/safe_call.h:13-23).
+ *
+ * Images are device pointers with a row pitch in BYTES.  Poses are 4x4
+ * row-major double matrices T_wc (camera -> world), the matrix form of the
+ * reference's Sophus::SE3d frame poses.  `stream` is a cudaStream_t passed as
+ * void* (NULL = legacy default stream).
+ *
+ * Mapping of reference interfaces (paths relative to the reference project):
+ *   DenseMapping::DenseMapping(K)          include/voxel_hashing/voxel_hashing.h:15   -> gbf_session_create
+ *   DenseMapping::update(frame)            src/voxel_hashing/voxel_hashing.cpp:44-65  -> gbf_fuse (nmap given)
+ *   DenseMapping::update(depth,image,pose) src/voxel_hashing/voxel_hashing.cpp:67-85  -> gbf_fuse (nmap NULL)
+ *   DenseMapping::raycast                  src/voxel_hashing/voxel_hashing.cpp:87-119 -> gbf_raycast
+ *   DenseMapping::reset_mapping            src/voxel_hashing/voxel_hashing.cpp:137-140 -> gbf_session_reset
+ *   DenseMapping::fetch_mesh_*             src/voxel_hashing/voxel_hashing.cpp:142-187 -> gbf_extract_mesh
+ *   DenseMapping::write/readMapFromDisk    src/voxel_hashing/voxel_hashing.cpp:189-205 -> gbf_map_export / gbf_map_import
+ *   DeviceImage::upload                    src/tracking/device_image.cpp:146-181      -> gbf_build_pyramid
+ *   DenseTracking::compute_transform       src/tracking/icp_tracker.cpp:23-156        -> gbf_track
+ *   icp_reduce / rgb_step                  src/tracking/pose_estimator.cu:267-307,
+ *                                          src/tracking/m_estimator.cu:437-482        -> gbf_reduce
+ *   System::process_images                 src/system.cpp:40-114                      -> gbf_process_frame
+ */
+#ifndef GBFUSION_H
+#define GBFUSION_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GBF_API __attribute__((visibility("default")))
+#else
+#define GBF_API
+#endif
+
+#define GBF_MAX_LEVELS 5
+#define GBF_BLOCK_SIDE 8
+#define GBF_BLOCK_VOXELS 512
+
+typedef enum gbf_status {
+    GBF_OK = 0,
+    GBF_ERR_INVALID_ARG = 1,  /* bad pointer, size or configuration          */
+    GBF_ERR_CUDA = 2,         /* a CUDA runtime call failed                   */
+    GBF_ERR_OUT_OF_MEMORY = 3,/* device allocation failed                     */
+    GBF_ERR_CAPACITY = 4,     /* batch slot / output buffer too small         */
+    GBF_ERR_NO_DEVICE = 5     /* no CUDA device visible                       */
+} gbf_status;
+
+/* Per-session device status bits (sticky until gbf_session_reset). */
+enum {
+    GBF_FLAG_POOL_EXHAUSTED = 1u << 0, /* block pool full: blocks were not allocated */
+    GBF_FLAG_HASH_FULL      = 1u << 1, /* probe limit hit: blocks were not allocated */
+    GBF_FLAG_COORD_RANGE    = 1u << 2, /* block coordinate outside +-2^20            */
+    GBF_FLAG_TRACK_FAILED   = 1u << 3, /* last frame's tracking failed (pose kept)   */
+    GBF_FLAG_NAN_POSE       = 1u << 4  /* solver produced a non-finite pose          */
+};
+
+typedef enum gbf_voxel_layout {
+    GBF_VOXEL_REF = 0,  /* int16 sdf (x32767, truncating) + f32 weight (<=255) + rgb8:
+                           the reference Voxel semantics, include/data_struct/voxel.h:11-66 */
+    GBF_VOXEL_HALF = 1  /* fp16 sdf + u16 weight (w*256, <=255) + rgb8: 8 B per voxel */
+} gbf_voxel_layout;
+
+typedef enum gbf_mesh_mode {
+    GBF_MESH_VERTEX = 0, /* fetch_mesh_vertex_only  */
+    GBF_MESH_NORMAL = 1, /* fetch_mesh_with_normal  */
+    GBF_MESH_COLOUR = 2  /* fetch_mesh_with_colour  */
+} gbf_mesh_mode;
+
+/* IntrinsicMatrix, include/data_struct/intrinsic_matrix.h:12-20 (invfx/invfy derived). */
+typedef struct gbf_intrinsics {
+    int32_t width, height;
+    float fx, fy, cx, cy;
+} gbf_intrinsics;
+
+/* MapState (include/data_struct/map_struct.h:17-51) + TrackingContext
+ * (include/tracking/icp_tracker.h:20-26) + the thresholds the reference
+ * hard-codes (pose_estimator.cu:292-293, icp_tracker.cpp:89-90). */
+typedef struct gbf_config {
+    float voxel_size;     /* metres                                               */
+    float truncation;     /* metres (reference hard-codes 5*voxel_size)           */
+    float zmin_update, zmax_update, zmin_raycast, zmax_raycast;
+    int32_t num_buckets;  /* hash slots (power of two not required)               */
+    int32_t num_blocks;   /* block pool size                                      */
+    int32_t voxel_layout; /* gbf_voxel_layout                                     */
+    int32_t num_levels;   /* pyramid levels, 1..GBF_MAX_LEVELS                    */
+    int32_t max_iterations[GBF_MAX_LEVELS]; /* per level, level 0 = finest         */
+    float w_icp, w_rgb;   /* A = w_icp*H_icp + w_rgb*H_rgb (reference: 1e6, 1)    */
+    float icp_dist_thresh;  /* metres (reference 0.01)                            */
+    float icp_angle_thresh; /* compared with |n_c x n_l| (reference cos(30*3.14/180)) */
+    int32_t bilateral;    /* 1: bilateral-filter the tracking depth (reference)   */
+    int32_t max_probe;    /* hash probe limit (bounded insert/lookup)             */
+} gbf_config;
+
+typedef struct gbf_track_result {
+    int32_t success;      /* TrackingResult::sucess                               */
+    int32_t iterations;   /* Gauss-Newton iterations actually run                 */
+    float icp_error, rgb_error;
+    float icp_inliers, rgb_inliers; /* correspondences of the last iteration       */
+    double update[16];    /* TrackingResult::update (T_ref<-cur), row-major 4x4   */
+} gbf_track_result;
+
+typedef struct gbf_frame_stats {
+    int64_t frame_index;
+    int32_t allocated_blocks;
+    int32_t visible_blocks;
+    int32_t render_blocks_valid;
+    uint32_t status;      /* GBF_FLAG_* bits                                      */
+    gbf_track_result track;
+} gbf_frame_stats;
+
+typedef struct gbf_session gbf_session;
+typedef struct gbf_batch gbf_batch;
+typedef struct gbf_synth_scene gbf_synth_scene;
+
+/* ---- library ---------------------------------------------------------------- */
+GBF_API const char *gbf_version(void);
+GBF_API const char *gbf_last_error(void);
+/* Fills the reference's MapStruct defaults (src/data_struct/map_struct.cu:17-35),
+ * with truncation = 5*voxel as MapState::truncation_dist (map_struct.cu:120-123),
+ * a 3-level 10/5/3 pyramid and the reference tracking thresholds. */
+GBF_API gbf_status gbf_config_default(gbf_config *cfg);
+/* Device bytes one session needs (admission control); host-only, no GPU. */
+GBF_API gbf_status gbf_session_bytes(const gbf_config *cfg, const gbf_intrinsics *K, uint64_t *bytes);
+
+/* ---- session: DenseMapping + DenseOdometry state on one GPU ---------------- */
+GBF_API gbf_status gbf_session_create(const gbf_config *cfg, const gbf_intrinsics *K, gbf_session **out);
+GBF_API gbf_status gbf_session_destroy(gbf_session *s);
+GBF_API gbf_status gbf_session_reset(gbf_session *s, void *stream);
+/* Device input staging buffers owned by the session (u16 depth in mm, pitch
+ * width*2; rgb8 packed, pitch width*3), filled by the caller before
+ * gbf_process_frame_staged / gbf_batch_process. */
+GBF_API gbf_status gbf_session_inputs(gbf_session *s, uint16_t **depth_mm_dev, uint8_t **rgb_dev);
+/* Copy one frame (host -- pinned for an asynchronous copy -- or device memory)
+ * into the session's staging buffers on `stream`. */
+GBF_API gbf_status gbf_session_stage(gbf_session *s, const uint16_t *depth_mm, int64_t depth_pitch,
+                                     const uint8_t *rgb, int64_t rgb_pitch, void *stream);
+GBF_API gbf_status gbf_set_pose(gbf_session *s, const double T_wc[16], void *stream);
+GBF_API gbf_status gbf_get_pose(gbf_session *s, double T_wc[16], void *stream);
+GBF_API gbf_status gbf_get_stats(gbf_session *s, gbf_frame_stats *out, void *stream);
+
+/* ---- mapping ------------------------------------------------------------------ */
+/* Allocate blocks along every valid pixel's truncation band, enumerate visible
+ * blocks and integrate TSDF + colour.  depth: float metres.  rgb: 3 bytes/px.
+ * nmap != NULL selects the normal-weighted update (update_map_weighted_kernel,
+ * depth_fusion.cu:356-428), NULL the 1/d^2 update (update_map_with_colour_kernel,
+ * depth_fusion.cu:288-354). */
+GBF_API gbf_status gbf_fuse(gbf_session *s, const float *depth_dev, int64_t depth_pitch,
+                            const uint8_t *rgb_dev, int64_t rgb_pitch,
+                            const float *nmap_dev, int64_t nmap_pitch,
+                            const double T_wc[16], void *stream);
+/* z-range tiles from the last fuse's visible blocks, then a per-pixel raycast
+ * into vmap (float4 per pixel, NaN = no hit).  As in the reference, vmap is left
+ * untouched when the last fuse saw no visible / renderable block. */
+GBF_API gbf_status gbf_raycast(gbf_session *s, const double T_wc[16],
+                               float *vmap_dev, int64_t vmap_pitch, void *stream);
+/* Marching cubes over all allocated blocks into caller-allocated device
+ * buffers (3 float3 per triangle; attr: 3 float3 normals or 3 uchar3 colours).
+ * *n_tris receives the triangle count clamped to max_tris (synchronises). */
+GBF_API gbf_status gbf_extract_mesh(gbf_session *s, int32_t mode, float *vertex_dev, void *attr_dev,
+                                    uint64_t max_tris, uint64_t *n_tris, void *stream);
+
+/* ---- tracking ----------------------------------------------------------------- */
+/* Build the intensity / vertex / normal pyramids of a frame into the session's
+ * `current` image set (which=0) or `reference` set (which=1). */
+GBF_API gbf_status gbf_build_pyramid(gbf_session *s, int32_t which, const float *depth_dev, int64_t depth_pitch,
+                                     const uint8_t *rgb_dev, int64_t rgb_pitch, void *stream);
+/* One ICP + photometric reduction at `level` for pose T (T_cur<-ref, float
+ * cast as the reference) and photometric stddev: out[0..28] ICP sums, out[29..57]
+ * RGB sums in the create_jtjjtr packing (reduce_sum.h:48-61). Synchronises. */
+GBF_API gbf_status gbf_reduce(gbf_session *s, int32_t level, const double T[16], float stddev,
+                              double out[58], void *stream);
+/* Coarse-to-fine Gauss-Newton between the reference and current sets. Synchronises. */
+GBF_API gbf_status gbf_track(gbf_session *s, const double init[16], gbf_track_result *out, void *stream);
+/* Copy one pyramid image: kind 0 vmap, 1 nmap (float4), 2 intensity, 3 dI/dx,
+ * 4 dI/dy, 5 filtered depth (float). which: 0 current, 1 reference. */
+GBF_API gbf_status gbf_get_image(gbf_session *s, int32_t which, int32_t kind, int32_t level,
+                                 void *out_dev, int64_t pitch, void *stream);
+
+/* ---- full frame: System::process_images -------------------------------------- */
+/* ingest (u16 mm -> m, rgb -> gray, pyramids) -> track against the model
+ * prediction -> fuse raw depth at the new pose -> raycast the new reference
+ * vertex map -> rebuild its pyramid.  No host synchronisation. */
+GBF_API gbf_status gbf_process_frame(gbf_session *s, const uint16_t *depth_mm_dev, int64_t depth_pitch,
+                                     const uint8_t *rgb_dev, int64_t rgb_pitch, void *stream);
+/* Same, from the session's own staging buffers (gbf_session_inputs). */
+GBF_API gbf_status gbf_process_frame_staged(gbf_session *s, void *stream);
+
+/* ---- map export / import (canonical per-block form) ---------------------------- */
+/* Allocated blocks: coords[3*i] block position, sdf/weight float per voxel
+ * (512 per block, index z*64+y*8+x), rgb 3 bytes per voxel.  Synchronises. */
+GBF_API gbf_status gbf_map_export(gbf_session *s, int32_t *coords, float *sdf, float *weight, uint8_t *rgb,
+                                  int64_t max_blocks, int64_t *n_blocks);
+GBF_API gbf_status gbf_map_import(gbf_session *s, const int32_t *coords, const float *sdf, const float *weight,
+                                  const uint8_t *rgb, int64_t n_blocks);
+/* Visible-block list of the last fuse (block coordinates), synchronises. */
+GBF_API gbf_status gbf_visible_blocks(gbf_session *s, int32_t *coords, int64_t max_blocks, int64_t *n_blocks);
+/* z-range grid of the last raycast: 2 floats per cell (min, max), (H/8)x(W/8). */
+GBF_API gbf_status gbf_zrange(gbf_session *s, float *out_host, int64_t max_cells);
+
+/* ---- batch: many sessions per launch ----------------------------------------- */
+GBF_API gbf_status gbf_batch_create(int32_t max_sessions, gbf_batch **out);
+GBF_API gbf_status gbf_batch_destroy(gbf_batch *b);
+GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s);
+/* One frame for every slot with active[slot] != 0, from each session's staging
+ * buffers, all sessions in the same launches; replayed from a CUDA graph when
+ * use_graph != 0 (captured on first use for the current slot assignment). */
+GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_t use_graph, void *stream);
+/* Read slot `slot`'s next frames straight from device buffers (dense u16 depth
+ * and rgb8 of the session's size) instead of its staging buffers; the pointers
+ * are taken at each gbf_batch_process call (NULL, NULL restores staging). */
+GBF_API gbf_status gbf_batch_set_inputs(gbf_batch *b, int32_t slot, const uint16_t *depth_dev, const uint8_t *rgb_dev);
+/* Record CUDA events at the phase boundaries of every tick (captured into the
+ * graph): ingest, track, alloc+visible, integrate, z-range, march, post. */
+GBF_API gbf_status gbf_batch_set_timing(gbf_batch *b, int32_t enable);
+/* Mean durations (ms) of the 7 phases over the ticks since timing was enabled
+ * (waits for the outstanding ticks); ms[7], when n > 7, receives the tick count. */
+GBF_API gbf_status gbf_batch_phase_ms(gbf_batch *b, float *ms, int32_t n);
+/* Number of kernel launches one tick makes. */
+GBF_API gbf_status gbf_batch_kernels(gbf_batch *b, int32_t *n);
+
+/* ---- synthetic RGB-D scenes (test and benchmark input) ------------------------ */
+typedef struct gbf_synth_params {
+    float room[3];       /* box room extent x, y, z (metres); z up            */
+    int32_t n_spheres, n_boxes;
+    float sphere_rmin, sphere_rmax;
+    uint64_t seed;
+    int32_t trajectory;  /* 0 circle (r, height, yaw jitter), 1 figure-eight   */
+    float radius, height, yaw_jitter_deg, speed; /* speed in m/s for figure-eight */
+    float fps;
+    int32_t frames_per_loop;
+    float noise;         /* 1 = depth noise sigma 0.0012+0.0019(z-0.4)^2, 0 = none */
+    float zclip_min, zclip_max;
+} gbf_synth_params;
+
+GBF_API gbf_status gbf_synth_default(gbf_synth_params *p);
+GBF_API gbf_status gbf_synth_create(const gbf_synth_params *p, gbf_synth_scene **out);
+GBF_API gbf_status gbf_synth_destroy(gbf_synth_scene *sc);
+GBF_API gbf_status gbf_synth_pose(const gbf_synth_scene *sc, int32_t frame, double T_wc[16]);
+GBF_API gbf_status gbf_synth_render(const gbf_synth_scene *sc, const gbf_intrinsics *K, const double T_wc[16],
+                                    int32_t frame, uint16_t *depth_mm_dev, uint8_t *rgb_dev, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBFUSION_H */

@@ -1,0 +1,236 @@
+// gbf_device.cuh -- device helpers shared by the kernels.
+//
+// Arithmetic follows the reference's expression order exactly; the library is
+// compiled with -fmad=false so that no multiply-add is contracted and every
+// float operation rounds as written (the oracle uses -ffp-contract=off).
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbf_types.h"
+#include "../../include/gbfusion.h"
+
+namespace gbf {
+
+// ---------------------------------------------------------------------------
+// float 3x4 rigid transform, rows (R0|t0), (R1|t1), (R2|t2)
+// Matrix3x4::operator()(Vector3) (include/math/matrix_type.h:96-100): each row
+// is a Vector4 dot with (x, y, z, 1), summed left to right.
+struct M34 {
+    float m[12];
+    __device__ __forceinline__ float3 apply(float x, float y, float z) const {
+        return make_float3(((m[0] * x + m[1] * y) + m[2] * z) + m[3] * 1.0f,
+                           ((m[4] * x + m[5] * y) + m[6] * z) + m[7] * 1.0f,
+                           ((m[8] * x + m[9] * y) + m[10] * z) + m[11] * 1.0f);
+    }
+    // Matrix3x4::rotate (matrix_type.h:88-94)
+    __device__ __forceinline__ float3 rotate(float x, float y, float z) const {
+        return make_float3((m[0] * x + m[1] * y) + m[2] * z,
+                           (m[4] * x + m[5] * y) + m[6] * z,
+                           (m[8] * x + m[9] * y) + m[10] * z);
+    }
+};
+
+__device__ __forceinline__ M34 pose_to_float(const double *p) {
+    M34 r;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) r.m[i] = (float)p[i];
+    return r;
+}
+
+// SE3 inverse in double: (R^T, -(R^T t)); sums left to right.
+__device__ __forceinline__ void pose_inverse(const double *p, double *o) {
+    o[0] = p[0]; o[1] = p[4]; o[2] = p[8];
+    o[4] = p[1]; o[5] = p[5]; o[6] = p[9];
+    o[8] = p[2]; o[9] = p[6]; o[10] = p[10];
+    o[3] = -((o[0] * p[3] + o[1] * p[7]) + o[2] * p[11]);
+    o[7] = -((o[4] * p[3] + o[5] * p[7]) + o[6] * p[11]);
+    o[11] = -((o[8] * p[3] + o[9] * p[7]) + o[10] * p[11]);
+}
+
+// c = a * b
+__device__ __forceinline__ void pose_mul(const double *a, const double *b, double *c) {
+    double r[12];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            r[i * 4 + j] = (a[i * 4 + 0] * b[0 * 4 + j] + a[i * 4 + 1] * b[1 * 4 + j]) + a[i * 4 + 2] * b[2 * 4 + j];
+        r[i * 4 + 3] = ((a[i * 4 + 0] * b[3] + a[i * 4 + 1] * b[7]) + a[i * 4 + 2] * b[11]) + a[i * 4 + 3];
+    }
+#pragma unroll
+    for (int i = 0; i < 12; ++i) c[i] = r[i];
+}
+
+__device__ __forceinline__ void pose_identity(double *p) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) p[i] = (i == 0 || i == 5 || i == 10) ? 1.0 : 0.0;
+}
+
+__device__ __forceinline__ void pose_copy(const double *a, double *b) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) b[i] = a[i];
+}
+
+// ---------------------------------------------------------------------------
+// Vector3 helpers in the reference's order (include/math/vector_type.h)
+__device__ __forceinline__ float norm3(float x, float y, float z) {
+    return sqrtf((x * x + y * y) + z * z);
+}
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+
+// ToVector3i (vector_type.h:218-225): truncate, then step down when above.
+__device__ __forceinline__ int floor_ref(float v) {
+    int b = __float2int_rz(v);
+    return ((float)b > v) ? b - 1 : b;
+}
+
+// voxelPosToBlockPos (map_struct.cu:626-636)
+__device__ __forceinline__ int voxel_to_block(int v) { return (v < 0 ? v - 7 : v) / 8; }
+// voxelPosToLocalPos (map_struct.cu:643-655)
+__device__ __forceinline__ int voxel_to_local(int v) {
+    int r = v % 8;
+    return r < 0 ? r + 8 : r;
+}
+
+// computeHash (map_struct.cu:143-148) with defined 32-bit wraparound.
+__host__ __device__ __forceinline__ int compute_hash(int x, int y, int z, int n) {
+    unsigned ux = (unsigned)x * 73856093u, uy = (unsigned)y * 19349669u, uz = (unsigned)z * 83492791u;
+    int res = (int)(ux ^ uy ^ uz);
+    res %= n;
+    return res < 0 ? res + n : res;
+}
+
+__host__ __device__ __forceinline__ unsigned long long pack_key(int x, int y, int z) {
+    const unsigned long long m = (1ull << kCoordBits) - 1ull;
+    return (((unsigned long long)(unsigned)x & m) << (2 * kCoordBits)) |
+           (((unsigned long long)(unsigned)y & m) << kCoordBits) | ((unsigned long long)(unsigned)z & m);
+}
+
+__device__ __forceinline__ bool coord_ok(int x, int y, int z) {
+    return x > -kCoordLimit && x < kCoordLimit && y > -kCoordLimit && y < kCoordLimit && z > -kCoordLimit &&
+           z < kCoordLimit;
+}
+
+// Read-only lookup: pool block id or -1.
+__device__ __forceinline__ int find_block(const SessionView &sv, int bx, int by, int bz) {
+    if (!coord_ok(bx, by, bz)) return -1;
+    const unsigned long long key = pack_key(bx, by, bz);
+    int slot = compute_hash(bx, by, bz, sv.cap);
+    for (int p = 0; p < sv.max_probe; ++p) {
+        const int4 e = __ldg(reinterpret_cast<const int4 *>(sv.table) + slot);
+        const unsigned long long k = ((unsigned long long)(unsigned)e.y << 32) | (unsigned)e.x;
+        if (k == key) return e.z;
+        if (k == kEmptyKey) return -1;
+        slot = (slot + 1 == sv.cap) ? 0 : slot + 1;
+    }
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Voxel storage.  REF: int16 sdf packed as (short)(v*32767) (truncation),
+// unpacked as v/32767.f; float weight clamped to 255 (include/data_struct/
+// voxel.h:36-66).  HALF: fp16 sdf (round to nearest), weight as uint16 w*256
+// rounded to nearest, clamped to 255*256.
+struct Vox {
+    float sdf;
+    float w;
+    uchar4 rgb;
+};
+
+__device__ __forceinline__ float sdf_ref_unpack(short v) { return (float)v / 32767.f; }
+__device__ __forceinline__ short sdf_ref_pack(float v) { return (short)__float2int_rz(v * 32767.f); }
+__device__ __forceinline__ float weight_ref_store(float w) { return w > 255.f ? 255.f : w; }
+__device__ __forceinline__ unsigned short weight_half_pack(float w) {
+    float q = w * 256.f + 0.5f;
+    if (!(q < 65280.f)) q = 65280.f;
+    return (unsigned short)__float2uint_rz(q);
+}
+__device__ __forceinline__ float weight_half_unpack(unsigned short q) { return (float)q * (1.0f / 256.f); }
+
+template <int LAYOUT>
+__device__ __forceinline__ Vox load_vox(const SessionView &sv, size_t i) {
+    Vox v;
+    if (LAYOUT == GBF_VOXEL_REF) {
+        v.sdf = sdf_ref_unpack(reinterpret_cast<const short *>(sv.vox_sdf)[i]);
+        v.w = reinterpret_cast<const float *>(sv.vox_w)[i];
+    } else {
+        v.sdf = __half2float(reinterpret_cast<const __half *>(sv.vox_sdf)[i]);
+        v.w = weight_half_unpack(reinterpret_cast<const unsigned short *>(sv.vox_w)[i]);
+    }
+    v.rgb = sv.vox_rgb[i];
+    return v;
+}
+
+// sdf + validity only (raycast / meshing).  Weight zero = unobserved.
+template <int LAYOUT>
+__device__ __forceinline__ float load_sdf(const SessionView &sv, size_t i, float &w) {
+    if (LAYOUT == GBF_VOXEL_REF) {
+        w = __ldg(reinterpret_cast<const float *>(sv.vox_w) + i);
+        return sdf_ref_unpack(__ldg(reinterpret_cast<const short *>(sv.vox_sdf) + i));
+    } else {
+        w = weight_half_unpack(__ldg(reinterpret_cast<const unsigned short *>(sv.vox_w) + i));
+        return __half2float(__ldg(reinterpret_cast<const __half *>(sv.vox_sdf) + i));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// status bits
+__device__ __forceinline__ void raise_flag(const SessionView &sv, unsigned bits) {
+    atomicOr(reinterpret_cast<unsigned *>(sv.ctr + C_STATUS), bits);
+}
+
+// warp-aggregated append: returns this lane's index in dst (all active lanes with pred).
+__device__ __forceinline__ int warp_append(int *counter, bool pred) {
+    const unsigned mask = __activemask();
+    const unsigned ballot = __ballot_sync(mask, pred);
+    if (!ballot) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ballot) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(ballot));
+    base = __shfl_sync(mask, base, leader);
+    return pred ? base + __popc(ballot & ((1u << lane) - 1u)) : -1;
+}
+
+// Insert (or find) one block in the session table; stamps it with `frame`.
+__device__ __forceinline__ int insert_block(const SessionView &sv, unsigned long long key, int bx, int by, int bz, int frame) {
+    int slot = compute_hash(bx, by, bz, sv.cap);
+    for (int p = 0; p < sv.max_probe; ++p) {
+        HashSlot *e = sv.table + slot;
+        unsigned long long k = __ldcg(&e->key);
+        if (k == kEmptyKey) {
+            k = atomicCAS(&e->key, kEmptyKey, key);
+            if (k == kEmptyKey) {
+                // this thread owns the new slot: take a pool block
+                const int id = atomicAdd(sv.ctr + C_NUSED, 1);
+                if (id < sv.pool) {
+                    sv.bcoord[id] = make_int4(bx, by, bz, slot);
+                    sv.bstamp[id] = frame;
+                    sv.bfresh[id] = 1;
+                    __stcg(&e->ptr, id);
+                    return id;
+                }
+                raise_flag(sv, GBF_FLAG_POOL_EXHAUSTED);
+                return -1;
+            }
+        }
+        if (k == key) {
+            // existing block; a concurrent creator stamps its own block, so a
+            // pending (-1) id needs no wait
+            const int id = __ldcg(&e->ptr);
+            if (id >= 0) sv.bstamp[id] = frame;
+            return id;
+        }
+        slot = (slot + 1 == sv.cap) ? 0 : slot + 1;
+    }
+    raise_flag(sv, GBF_FLAG_HASH_FULL);
+    return -1;
+}
+
+}  // namespace gbf

@@ -1,0 +1,71 @@
+// gbf_internal.h -- host runtime internals (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/gbfusion.h"
+#include "gbf_kernels.h"
+#include "gbf_types.h"
+
+namespace gbf {
+
+struct M34Host {
+    float m[12];
+};
+
+gbf_status set_error(gbf_status st, const char *msg);
+gbf_status cuda_error(cudaError_t e, const char *where);
+// cudaGetLastError after a launch sequence
+gbf_status check_cuda(const char *where);
+
+// Byte layout of one session's device arena.
+struct ArenaLayout {
+    size_t total;
+    size_t table, bcoord, bstamp, bfresh, vis, mesh_off, vox_sdf, vox_w, vox_rgb, ctr, ts;
+    size_t in_depth, in_rgb, depth_raw, rgb4, nmap_ext, zr_min, zr_max, partials;
+    size_t depth[kMaxLevels], inten[2][kMaxLevels], gx[kMaxLevels], gy[kMaxLevels];
+    size_t vmap[2][kMaxLevels], nmap[2][kMaxLevels];
+};
+
+gbf_status validate(const gbf_config *cfg, const gbf_intrinsics *K);
+ArenaLayout plan_arena(const gbf_config &cfg, const gbf_intrinsics &K);
+int reduce_ctas(int pixels);
+
+}  // namespace gbf
+
+struct gbf_session {
+    gbf_config cfg;
+    gbf_intrinsics K;
+    void *arena = nullptr;
+    gbf::ArenaLayout lay;
+    gbf::SessionView view;            // host copy (active = 1)
+    gbf::SessionView *d_view = nullptr; // device copy for single-session launches
+    gbf::Extent ex;
+    int layouts[2] = {0, 0};
+    int device = 0;
+};
+
+struct gbf_batch {
+    int max_slots = 0;
+    std::vector<gbf_session *> sessions;
+    std::vector<uint16_t *> in_depth;  // per-slot input override (device, dense)
+    std::vector<uint8_t *> in_rgb;
+    gbf::SessionView *h_views[2] = {nullptr, nullptr}; // pinned mirrors (ping-pong)
+    gbf::SessionView *d_views = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    bool ev_used[2] = {false, false};
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaStream_t own = nullptr;
+    int flip = 0;
+    int nslots = 0;
+    gbf::Extent ex;
+    int layouts[2] = {0, 0};
+    int timing = 0;
+    int last = -1;
+    cudaEvent_t pev[2][8] = {};   // phase boundaries per mirror (captured into the graphs)
+    int pending[2] = {0, 0};      // phase events recorded but not yet read
+    double phase_sum[8] = {};
+    long long phase_n = 0;
+};

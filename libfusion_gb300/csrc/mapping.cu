@@ -1,0 +1,323 @@
+// mapping.cu -- block allocation, visible-block enumeration and TSDF/colour
+// integration (src/voxel_hashing/depth_fusion.cu:15-575 and the hash core of
+// src/data_struct/map_struct.cu:143-389).
+//
+// GB300 design, per frame and for every session of a batch:
+//   fuse_begin  bump the session's fuse counter, clear the visible count.
+//   alloc       one thread per level-0 pixel walks the blocks of its truncation
+//               band (3-D Bresenham, depth_fusion.cu:121-228); the CTA dedupes
+//               the keys of its 16x16 pixel tile in a shared-memory set and each
+//               unique key is inserted once into the session's open-addressing
+//               table with a 64-bit CAS (lock-free, no dropped blocks), stamping
+//               the block with the fuse counter.
+//   visible     one thread per ALLOCATED block (not per table slot): visible =
+//               stamped this fuse OR a block corner projects into the image
+//               within [zmin, zmax] (is_block_visible, depth_fusion.cu:15-47);
+//               warp-aggregated append to the visible list.
+//   integrate   one CTA per visible block (grid-stride), 2 voxels per thread,
+//               coalesced SoA voxel read-modify-write; blocks allocated this
+//               fuse skip the read and are written whole (lazy zeroing instead
+//               of the reference's full-pool cudaMemset, map_struct.cu:90).
+#include "gbf_device.cuh"
+#include "gbf_kernels.h"
+
+namespace gbf {
+
+namespace {
+
+constexpr int kAllocTile = 16;        // 16x16 pixels per CTA
+constexpr int kSetSize = 1024;        // shared-memory key set per CTA
+
+__global__ void fuse_begin_kernel(const SessionView *svs) {
+    const SessionView &sv = svs[blockIdx.x];
+    if (!sv.active || threadIdx.x != 0) return;
+    sv.ctr[C_FRAME] += 1;
+    sv.ctr[C_NVIS] = 0;
+}
+
+__global__ void fuse_import_kernel(const SessionView *svs, FuseImport in) {
+    const SessionView &sv = svs[0];
+    const int W = sv.lv[0].w, H = sv.lv[0].h;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * H) return;
+    const int x = i % W, y = i / W;
+    sv.depth_raw[i] = reinterpret_cast<const float *>(reinterpret_cast<const char *>(in.depth) + y * in.depth_pitch)[x];
+    const uint8_t *px = in.rgb + y * in.rgb_pitch + (size_t)x * 3;
+    sv.rgb4[i] = make_uchar4(px[0], px[1], px[2], 0);
+    if (in.nmap)
+        sv.nmap_ext[i] = reinterpret_cast<const float4 *>(reinterpret_cast<const char *>(in.nmap) + y * in.nmap_pitch)[x];
+}
+
+// Shared-memory set insert; false when the set is full (caller inserts globally).
+__device__ __forceinline__ bool set_insert(unsigned long long *set, unsigned long long key) {
+    unsigned h = (unsigned)(key ^ (key >> 29) ^ (key >> 43)) * 0x9E3779B1u;
+    unsigned s = h >> (32 - 10);  // kSetSize = 1024
+    for (int p = 0; p < 64; ++p) {
+        const unsigned long long old = atomicCAS(set + s, kEmptyKey, key);
+        if (old == kEmptyKey || old == key) return true;
+        s = (s + 1) & (kSetSize - 1);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void visit_block(const SessionView &sv, unsigned long long *set, int bx, int by, int bz,
+                                            int frame) {
+    if (!coord_ok(bx, by, bz)) {
+        raise_flag(sv, GBF_FLAG_COORD_RANGE);
+        return;
+    }
+    const unsigned long long key = pack_key(bx, by, bz);
+    if (!set_insert(set, key)) insert_block(sv, key, bx, by, bz, frame);
+}
+
+// unproject_world (depth_fusion.cu:101-112) then worldPtToVoxelPos + voxelPosToBlockPos
+__device__ __forceinline__ int3 pixel_block(const SessionView &sv, const M34 &T, int x, int y, float z) {
+    const LevelK &K = sv.lv[0];
+    const float px = (K.invfx * ((float)x - K.cx)) * z;
+    const float py = (K.invfy * ((float)y - K.cy)) * z;
+    const float3 w = T.apply(px, py, z);
+    return make_int3(voxel_to_block(floor_ref(w.x / sv.voxel)), voxel_to_block(floor_ref(w.y / sv.voxel)),
+                     voxel_to_block(floor_ref(w.z / sv.voxel)));
+}
+
+__global__ void __launch_bounds__(kAllocTile *kAllocTile) alloc_kernel(const SessionView *svs) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active) return;
+    const int W = sv.lv[0].w, H = sv.lv[0].h;
+    const int tiles_x = (W + kAllocTile - 1) / kAllocTile;
+    const int x = (blockIdx.x % tiles_x) * kAllocTile + (threadIdx.x % kAllocTile);
+    const int y = (blockIdx.x / tiles_x) * kAllocTile + (threadIdx.x / kAllocTile);
+    if ((blockIdx.x / tiles_x) * kAllocTile >= H) return;  // uniform per CTA
+
+    __shared__ unsigned long long set[kSetSize];
+    __shared__ M34 T;
+    for (int i = threadIdx.x; i < kSetSize; i += blockDim.x) set[i] = kEmptyKey;
+    if (threadIdx.x == 0) T = pose_to_float(sv.ts->map_pose);
+    __syncthreads();
+    const int frame = sv.ctr[C_FRAME];
+
+    if (x < W && y < H) {
+        const float z = sv.depth_raw[(size_t)y * W + x];
+        // create_blocks_kernel (depth_fusion.cu:130-141)
+        if (!(isnan(z) || z < sv.zmin_u || z > sv.zmax_u)) {
+            const float z_thresh = sv.tau * 0.5f;
+            const float z_near = fmaxf(sv.zmin_u, z - z_thresh);
+            const float z_far = fminf(sv.zmax_u, z + z_thresh);
+            if (z_near < z_far) {
+                int3 bn = pixel_block(sv, T, x, y, z_near);
+                const int3 bf = pixel_block(sv, T, x, y, z_far);
+                const int3 d = make_int3(bf.x - bn.x, bf.y - bn.y, bf.z - bn.z);
+                const int3 inc = make_int3(d.x < 0 ? -1 : 1, d.y < 0 ? -1 : 1, d.z < 0 ? -1 : 1);
+                const int3 ab = make_int3(abs(d.x), abs(d.y), abs(d.z));
+                const int3 e2 = make_int3(ab.x << 1, ab.y << 1, ab.z << 1);
+                visit_block(sv, set, bn.x, bn.y, bn.z, frame);
+                // Bresenham's line over block coordinates (depth_fusion.cu:153-227)
+                if (ab.x >= ab.y && ab.x >= ab.z) {
+                    int err1 = e2.y - 1, err2 = e2.z - 1;
+                    for (int i = 0; i < ab.x; ++i) {
+                        if (err1 > 0) { bn.y += inc.y; err1 -= e2.x; }
+                        if (err2 > 0) { bn.z += inc.z; err2 -= e2.x; }
+                        err1 += e2.y; err2 += e2.z; bn.x += inc.x;
+                        visit_block(sv, set, bn.x, bn.y, bn.z, frame);
+                    }
+                } else if (ab.y >= ab.x && ab.y >= ab.z) {
+                    int err1 = e2.x - 1, err2 = e2.z - 1;
+                    for (int i = 0; i < ab.y; ++i) {
+                        if (err1 > 0) { bn.x += inc.x; err1 -= e2.y; }
+                        if (err2 > 0) { bn.z += inc.z; err2 -= e2.y; }
+                        err1 += e2.x; err2 += e2.z; bn.y += inc.y;
+                        visit_block(sv, set, bn.x, bn.y, bn.z, frame);
+                    }
+                } else {
+                    int err1 = e2.y - 1, err2 = e2.x - 1;
+                    for (int i = 0; i < ab.z; ++i) {
+                        if (err1 > 0) { bn.y += inc.y; err1 -= e2.z; }
+                        if (err2 > 0) { bn.x += inc.x; err2 -= e2.z; }
+                        err1 += e2.y; err2 += e2.x; bn.z += inc.z;
+                        visit_block(sv, set, bn.x, bn.y, bn.z, frame);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kSetSize; i += blockDim.x) {
+        const unsigned long long key = set[i];
+        if (key == kEmptyKey) continue;
+        // unpack the 21-bit fields (sign-extend)
+        const int bx = (int)((long long)(key << (64 - 3 * kCoordBits)) >> (64 - kCoordBits));
+        const int by = (int)((long long)(key << (64 - 2 * kCoordBits)) >> (64 - kCoordBits));
+        const int bz = (int)((long long)(key << (64 - kCoordBits)) >> (64 - kCoordBits));
+        insert_block(sv, key, bx, by, bz, frame);
+    }
+}
+
+// is_vertex_visible / is_block_visible (depth_fusion.cu:15-47)
+__device__ __forceinline__ bool block_in_frustum(const SessionView &sv, const M34 &Tcw, int bx, int by, int bz) {
+    const LevelK &K = sv.lv[0];
+    const float scale = sv.block_metric;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int cx = bx + ((c & 1) ? 1 : 0), cy = by + ((c & 2) ? 1 : 0), cz = bz + ((c & 4) ? 1 : 0);
+        const float3 p = Tcw.apply((float)cx * scale, (float)cy * scale, (float)cz * scale);
+        const float u = (K.fx * p.x) / p.z + K.cx;
+        const float v = (K.fy * p.y) / p.z + K.cy;
+        if (!(u < 0 || v < 0 || u > (float)(K.w - 1) || v > (float)(K.h - 1) || p.z < sv.zmin_u || p.z > sv.zmax_u))
+            return true;
+    }
+    return false;
+}
+
+__global__ void visible_kernel(const SessionView *svs) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active) return;
+    __shared__ M34 Tcw;
+    if (threadIdx.x == 0) {
+        double inv[12];
+        pose_inverse(sv.ts->map_pose, inv);
+        Tcw = pose_to_float(inv);
+    }
+    __syncthreads();
+    const int frame = sv.ctr[C_FRAME];
+    const int n = min(sv.ctr[C_NUSED], sv.pool);
+    const int stride = gridDim.x * blockDim.x;
+    // whole warps iterate together so the append stays warp-uniform
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int id = base + threadIdx.x;
+        bool vis = false;
+        int tag = 0;
+        if (id < n) {
+            const int4 c = sv.bcoord[id];
+            vis = (sv.bstamp[id] == frame) || block_in_frustum(sv, Tcw, c.x, c.y, c.z);
+            tag = sv.bfresh[id] ? (int)0x80000000 : 0;
+        }
+        const int pos = warp_append(sv.ctr + C_NVIS, vis);
+        if (vis) sv.vis[pos] = id | tag;
+    }
+}
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(256) integrate_kernel(const SessionView *svs, int mode) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active || sv.layout != LAYOUT) return;
+    __shared__ M34 Tcw;
+    if (threadIdx.x == 0) {
+        double inv[12];
+        pose_inverse(sv.ts->map_pose, inv);
+        Tcw = pose_to_float(inv);
+    }
+    __syncthreads();
+    const LevelK &K = sv.lv[0];
+    const int W = K.w, H = K.h;
+    const int nvis = sv.ctr[C_NVIS];
+    const float4 *nmap = (mode == 1) ? sv.nmap[sv.ts->idx][0] : sv.nmap_ext;
+    const float voxel = sv.voxel, tau = sv.tau, inv_tau = sv.inv_tau;
+
+    for (int b = blockIdx.x; b < nvis; b += gridDim.x) {
+        const int tagged = sv.vis[b];
+        const int id = tagged & 0x7fffffff;
+        const bool fresh = tagged < 0;
+        const int4 bc = sv.bcoord[id];
+#pragma unroll
+        for (int half_i = 0; half_i < 2; ++half_i) {
+            const int li = threadIdx.x + half_i * 256;
+            const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
+            const size_t vi = (size_t)id * kBlockVoxels + li;
+            const float3 p = Tcw.apply((float)(bc.x * 8 + lx) * voxel, (float)(bc.y * 8 + ly) * voxel,
+                                       (float)(bc.z * 8 + lz) * voxel);
+            const int u = __float2int_rd(((K.fx * p.x) / p.z + K.cx) + 0.5f);
+            const int v = __float2int_rd(((K.fy * p.y) / p.z + K.cy) + 0.5f);
+            bool upd = !(u < 0 || v < 0 || u > W - 1 || v > H - 1);
+            float dist = 0.f, nz = 0.f, sdf = 0.f;
+            if (upd) {
+                dist = sv.depth_raw[(size_t)v * W + u];
+                if (mode == 0) {
+                    upd = !(isnan(dist) || (double)dist < 1e-2 || dist > sv.zmax_u || dist < sv.zmin_u);
+                } else {
+                    const float4 n = nmap[(size_t)v * W + u];
+                    nz = n.z;
+                    upd = !(isnan(dist) || isnan(n.x) || dist > sv.zmax_u || dist < sv.zmin_u);
+                }
+            }
+            if (upd) {
+                sdf = dist - p.z;
+                if (sdf < -tau) upd = false;
+            }
+            if (!upd) {
+                if (fresh) {
+                    if (LAYOUT == GBF_VOXEL_REF) {
+                        reinterpret_cast<short *>(sv.vox_sdf)[vi] = 0;
+                        reinterpret_cast<float *>(sv.vox_w)[vi] = 0.f;
+                    } else {
+                        reinterpret_cast<__half *>(sv.vox_sdf)[vi] = __float2half_rn(0.f);
+                        reinterpret_cast<unsigned short *>(sv.vox_w)[vi] = 0;
+                    }
+                    sv.vox_rgb[vi] = make_uchar4(0, 0, 0, 0);
+                }
+                continue;
+            }
+            sdf = fminf(1.0f, sdf * inv_tau);
+            Vox old;
+            if (fresh) {
+                old.sdf = 0.f; old.w = 0.f; old.rgb = make_uchar4(0, 0, 0, 0);
+            } else {
+                old = load_vox<LAYOUT>(sv, vi);
+            }
+            const float weight = (mode == 0) ? 1.0f / (dist * dist) : fabsf(sinf(nz)) / (dist * dist);
+            const uchar4 cn = sv.rgb4[(size_t)v * W + u];
+            float nsdf, nw;
+            uchar4 nrgb;
+            if (old.w == 0.f) {
+                nsdf = sdf; nw = weight; nrgb = cn;
+            } else {
+                nsdf = (old.sdf * old.w + sdf * weight) / (old.w + weight);
+                nw = old.w + weight;
+                const float den = old.w + weight;
+                nrgb.x = (unsigned char)__float2int_rz(((float)old.rgb.x * old.w + (float)cn.x * weight) / den);
+                nrgb.y = (unsigned char)__float2int_rz(((float)old.rgb.y * old.w + (float)cn.y * weight) / den);
+                nrgb.z = (unsigned char)__float2int_rz(((float)old.rgb.z * old.w + (float)cn.z * weight) / den);
+                nrgb.w = 0;
+            }
+            if (LAYOUT == GBF_VOXEL_REF) {
+                reinterpret_cast<short *>(sv.vox_sdf)[vi] = sdf_ref_pack(nsdf);
+                reinterpret_cast<float *>(sv.vox_w)[vi] = weight_ref_store(nw);
+            } else {
+                reinterpret_cast<__half *>(sv.vox_sdf)[vi] = __float2half_rn(nsdf);
+                reinterpret_cast<unsigned short *>(sv.vox_w)[vi] = weight_half_pack(nw);
+            }
+            sv.vox_rgb[vi] = nrgb;
+        }
+        if (fresh && threadIdx.x == 0) sv.bfresh[id] = 0;
+    }
+}
+
+}  // namespace
+
+void launch_fuse_import(const SessionView *d_sv, const Extent &ex, const FuseImport &in, cudaStream_t st) {
+    const int n = ex.w * ex.h;
+    fuse_import_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_sv, in);
+}
+
+void launch_alloc_visible(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {
+    fuse_begin_kernel<<<nslots, 32, 0, st>>>(d_sv);
+    const int tiles = ((ex.w + kAllocTile - 1) / kAllocTile) * ((ex.h + kAllocTile - 1) / kAllocTile);
+    alloc_kernel<<<dim3(tiles, nslots), kAllocTile * kAllocTile, 0, st>>>(d_sv);
+    const int gv = min(max((ex.max_pool + 255) / 256, 1), 1216);
+    visible_kernel<<<dim3(gv, nslots), 256, 0, st>>>(d_sv);
+}
+
+void launch_integrate(const SessionView *d_sv, int nslots, const Extent &ex, int mode, const int *layouts,
+                      cudaStream_t st) {
+    // one CTA per visible block, grid-stride; 8 resident CTAs of 256 threads per SM
+    const int gi = 152 * 8;
+    if (layouts[GBF_VOXEL_REF]) integrate_kernel<GBF_VOXEL_REF><<<dim3(gi, nslots), 256, 0, st>>>(d_sv, mode);
+    if (layouts[GBF_VOXEL_HALF]) integrate_kernel<GBF_VOXEL_HALF><<<dim3(gi, nslots), 256, 0, st>>>(d_sv, mode);
+}
+
+void launch_fuse(const SessionView *d_sv, int nslots, const Extent &ex, int mode, const int *layouts,
+                 cudaStream_t st) {
+    launch_alloc_visible(d_sv, nslots, ex, st);
+    launch_integrate(d_sv, nslots, ex, mode, layouts, st);
+}
+
+}  // namespace gbf

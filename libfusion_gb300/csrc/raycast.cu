@@ -1,0 +1,306 @@
+// raycast.cu -- z-range tiles and per-pixel raycast (src/voxel_hashing/
+// ray_tracing.cu:63-425) plus the post-raycast pyramid (DeviceImage::
+// resize_device_map, src/tracking/device_image.cpp:188-199).
+//
+// GB300 design:
+//   zr_init   z-range grid (H/8 x W/8) to (100, 0), render counter to 0.
+//   zrange    one thread per visible block: the block's screen box on the 1/8
+//             grid and its depth interval (create_rendering_block, :63-126), then
+//             integer atomicMin / atomicMax on the float bit patterns (all values
+//             are positive) of every covered cell.  The reference's 16x16
+//             rendering-tile list, its cudaMalloc and its host read-back
+//             (:223-277) are gone; the union of its tiles is exactly the box.
+//   raycast   one thread per pixel, warps on 16x2 pixel strips; the march of
+//             MapRenderingDelegate::operator() (:346-425) with a per-thread cache
+//             of the last block lookup so trilinear samples within one block
+//             cost one hash probe.  Output: camera-frame float4 vertex (NaN = miss).
+//   post      2x2 mean vertex pyramid, then normals of every level.
+#include "gbf_device.cuh"
+#include "gbf_kernels.h"
+
+namespace gbf {
+
+namespace {
+
+__global__ void zr_init_kernel(const SessionView *svs) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active) return;
+    const int n = sv.zr_w * sv.zr_h;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        sv.zr_min[i] = 100.f;
+        sv.zr_max[i] = 0.f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sv.ctr[C_RENDER] = 0;
+}
+
+__global__ void zrange_kernel(const SessionView *svs) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active) return;
+    __shared__ M34 Tcw;
+    if (threadIdx.x == 0) {
+        double inv[12];
+        pose_inverse(sv.ts->map_pose, inv);
+        Tcw = pose_to_float(inv);
+    }
+    __syncthreads();
+    const int nvis = sv.ctr[C_NVIS];
+    const LevelK &K = sv.lv[0];
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nvis; b += gridDim.x * blockDim.x) {
+        const int id = sv.vis[b] & 0x7fffffff;
+        const int4 bc = sv.bcoord[id];
+        int ulx = sv.zr_w, uly = sv.zr_h, lrx = -1, lry = -1;
+        float zx = sv.zmax_r, zy = sv.zmin_r;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int cx = bc.x + ((c & 1) ? 1 : 0), cy = bc.y + ((c & 2) ? 1 : 0), cz = bc.z + ((c & 4) ? 1 : 0);
+            const float3 p = Tcw.apply((float)cx * sv.block_metric, (float)cy * sv.block_metric,
+                                       (float)cz * sv.block_metric);
+            const float u = ((K.fx * p.x) / p.z + K.cx) / 8.0f;
+            const float v = ((K.fy * p.y) / p.z + K.cy) / 8.0f;
+            const float fu = floorf(u), fv = floorf(v), cu = ceilf(u), cv = ceilf(v);
+            if ((float)ulx > fu) ulx = __float2int_rz(fu);
+            if ((float)lrx < cu) lrx = __float2int_rz(cu);
+            if ((float)uly > fv) uly = __float2int_rz(fv);
+            if ((float)lry < cv) lry = __float2int_rz(cv);
+            if (zx > p.z) zx = p.z;
+            if (zy < p.z) zy = p.z;
+        }
+        if (ulx < 0) ulx = 0;
+        if (uly < 0) uly = 0;
+        if (lrx >= sv.zr_w) lrx = sv.zr_w - 1;
+        if (lry >= sv.zr_h) lry = sv.zr_h - 1;
+        if (ulx > lrx || uly > lry) continue;
+        if (zx < sv.zmin_r) zx = sv.zmin_r;
+        if (zy < sv.zmin_r) continue;
+        atomicAdd(sv.ctr + C_RENDER, 1);
+        const int ix = __float_as_int(zx), iy = __float_as_int(zy);
+        for (int y = uly; y <= lry; ++y)
+            for (int x = ulx; x <= lrx; ++x) {
+                atomicMin(reinterpret_cast<int *>(sv.zr_min) + y * sv.zr_w + x, ix);
+                atomicMax(reinterpret_cast<int *>(sv.zr_max) + y * sv.zr_w + x, iy);
+            }
+    }
+}
+
+struct BlockCache {
+    int bx, by, bz, id;
+};
+
+// read_sdf (ray_tracing.cu:291-305): nearest voxel, NaN when unallocated or unobserved
+template <int LAYOUT>
+__device__ __forceinline__ float read_sdf(const SessionView &sv, BlockCache &bc, float px, float py, float pz,
+                                          bool &valid) {
+    const int vx = floor_ref(px), vy = floor_ref(py), vz = floor_ref(pz);
+    const int bx = voxel_to_block(vx), by = voxel_to_block(vy), bz = voxel_to_block(vz);
+    if (bx != bc.bx || by != bc.by || bz != bc.bz) {
+        bc.bx = bx; bc.by = by; bc.bz = bz;
+        bc.id = find_block(sv, bx, by, bz);
+    }
+    if (bc.id >= 0) {
+        const size_t i = (size_t)bc.id * kBlockVoxels + (voxel_to_local(vz) * 64 + voxel_to_local(vy) * 8 +
+                                                          voxel_to_local(vx));
+        float w;
+        const float s = load_sdf<LAYOUT>(sv, i, w);
+        if (w != 0.f) {
+            valid = true;
+            return s;
+        }
+    }
+    valid = false;
+    return __int_as_float(0x7fffffff);
+}
+
+// read_sdf_interped (ray_tracing.cu:307-339)
+template <int LAYOUT>
+__device__ __forceinline__ float read_sdf_interped(const SessionView &sv, BlockCache &bc, float px, float py,
+                                                   float pz, bool &valid) {
+    const float fx = px - floorf(px), fy = py - floorf(py), fz = pz - floorf(pz);
+    bool vpt, v;
+    float s0, s1, r0, r1, r2, r3;
+    s0 = read_sdf<LAYOUT>(sv, bc, px, py, pz, vpt);
+    s1 = read_sdf<LAYOUT>(sv, bc, px + 1.0f, py + 0.0f, pz + 0.0f, v);
+    vpt &= v;
+    r0 = (1.0f - fx) * s0 + fx * s1;
+    s0 = read_sdf<LAYOUT>(sv, bc, px + 0.0f, py + 1.0f, pz + 0.0f, v);
+    vpt &= v;
+    s1 = read_sdf<LAYOUT>(sv, bc, px + 1.0f, py + 1.0f, pz + 0.0f, v);
+    vpt &= v;
+    r1 = (1.0f - fx) * s0 + fx * s1;
+    r2 = (1.0f - fy) * r0 + fy * r1;
+    s0 = read_sdf<LAYOUT>(sv, bc, px + 0.0f, py + 0.0f, pz + 1.0f, v);
+    vpt &= v;
+    s1 = read_sdf<LAYOUT>(sv, bc, px + 1.0f, py + 0.0f, pz + 1.0f, v);
+    vpt &= v;
+    r0 = (1.0f - fx) * s0 + fx * s1;
+    s0 = read_sdf<LAYOUT>(sv, bc, px + 0.0f, py + 1.0f, pz + 1.0f, v);
+    vpt &= v;
+    s1 = read_sdf<LAYOUT>(sv, bc, px + 1.0f, py + 1.0f, pz + 1.0f, v);
+    vpt &= v;
+    r1 = (1.0f - fx) * s0 + fx * s1;
+    r3 = (1.0f - fy) * r0 + fy * r1;
+    valid = vpt;
+    return (1.0f - fz) * r2 + fz * r3;
+}
+
+constexpr int kRayTileW = 16, kRayTileH = 16;
+constexpr int kMaxMarch = 1 << 16;  // safety bound; the march advances >= 1 voxel per step
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(kRayTileW *kRayTileH) raycast_kernel(const SessionView *svs, float4 *vmap_ext,
+                                                                       long long vmap_pitch) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active || sv.layout != LAYOUT) return;
+    // the reference skips the raycast when nothing was visible or renderable
+    if (sv.ctr[C_NVIS] == 0 || sv.ctr[C_RENDER] == 0) return;
+    const LevelK &K = sv.lv[0];
+    const int tiles_x = (K.w + kRayTileW - 1) / kRayTileW;
+    const int x = (blockIdx.x % tiles_x) * kRayTileW + (threadIdx.x % kRayTileW);
+    const int y = (blockIdx.x / tiles_x) * kRayTileH + (threadIdx.x / kRayTileW);
+    __shared__ M34 Twc, Tcw;
+    if (threadIdx.x == 0) {
+        double inv[12];
+        pose_inverse(sv.ts->map_pose, inv);
+        Tcw = pose_to_float(inv);
+        Twc = pose_to_float(sv.ts->map_pose);
+    }
+    __syncthreads();
+    if (x >= K.w || y >= K.h) return;
+
+    float4 *out = vmap_ext ? reinterpret_cast<float4 *>(reinterpret_cast<char *>(vmap_ext) + y * vmap_pitch) + x
+                           : sv.vmap[sv.ts->idx][0] + (size_t)y * K.w + x;
+    const float qnan = __int_as_float(0x7fffffff);
+    *out = make_float4(qnan, qnan, qnan, qnan);
+
+    const int cx = __float2int_rd((float)x / 8), cy = __float2int_rd((float)y / 8);
+    if (cx >= sv.zr_w || cy >= sv.zr_h) return;
+    const float zr0 = sv.zr_min[cy * sv.zr_w + cx], zr1 = sv.zr_max[cy * sv.zr_w + cx];
+    if ((double)zr1 < 1e-3 || (double)zr0 < 1e-3 || isnan(zr0) || isnan(zr1)) return;
+
+    const float iv = sv.inv_voxel;
+    // unproject (ray_tracing.cu:341-344): (x - cx) * invfx * z
+    float ux = (((float)x - K.cx) * K.invfx) * zr0, uy = (((float)y - K.cy) * K.invfy) * zr0;
+    float dist_s = norm3(ux, uy, zr0) * iv;
+    float3 bs = Twc.apply(ux, uy, zr0);
+    bs = make_float3(bs.x * iv, bs.y * iv, bs.z * iv);
+    ux = (((float)x - K.cx) * K.invfx) * zr1;
+    uy = (((float)y - K.cy) * K.invfy) * zr1;
+    const float dist_e = norm3(ux, uy, zr1) * iv;
+    float3 be = Twc.apply(ux, uy, zr1);
+    be = make_float3(be.x * iv, be.y * iv, be.z * iv);
+    float3 dir = make_float3(be.x - bs.x, be.y - bs.y, be.z - bs.z);
+    const float dn = norm3(dir.x, dir.y, dir.z);
+    dir = make_float3(dir.x / dn, dir.y / dn, dir.z / dn);
+    float3 r = bs;
+
+    BlockCache bc{0x7fffffff, 0x7fffffff, 0x7fffffff, -1};
+    float sdf = 1.0f, last_sdf, step;
+    bool valid = false;
+    for (int it = 0; dist_s < dist_e && it < kMaxMarch; ++it) {
+        last_sdf = sdf;
+        sdf = read_sdf<LAYOUT>(sv, bc, r.x, r.y, r.z, valid);
+        if (sdf <= 0.5f && sdf >= -0.5f) sdf = read_sdf_interped<LAYOUT>(sv, bc, r.x, r.y, r.z, valid);
+        if (sdf <= 0.0f) break;
+        if (sdf >= 0.f && last_sdf < 0.f) return;
+        step = valid ? fmaxf(sdf * sv.step_scale, 1.0f) : 2.0f;
+        r = make_float3(r.x + dir.x * step, r.y + dir.y * step, r.z + dir.z * step);
+        dist_s += step;
+    }
+    bool found = false;
+    if (sdf <= 0.0f) {
+        step = sdf * sv.step_scale;
+        r = make_float3(r.x + dir.x * step, r.y + dir.y * step, r.z + dir.z * step);
+        sdf = read_sdf_interped<LAYOUT>(sv, bc, r.x, r.y, r.z, valid);
+        step = sdf * sv.step_scale;
+        r = make_float3(r.x + dir.x * step, r.y + dir.y * step, r.z + dir.z * step);
+        found = valid;
+    }
+    if (found) {
+        const float3 c = Tcw.apply(r.x * sv.voxel, r.y * sv.voxel, r.z * sv.voxel);
+        *out = make_float4(c.x, c.y, c.z, 1.0f);
+    }
+}
+
+// cv::cuda::resize(vmap, 0.5): 2x2 mean of every channel
+__global__ void vmap_down_kernel(const SessionView *svs, int level) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active || level >= sv.levels) return;
+    const int w = sv.lv[level].w, h = sv.lv[level].h, pw = sv.lv[level - 1].w;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h) return;
+    const int x = i % w, y = i / w;
+    const int set = sv.ts->idx;
+    const float4 *s = sv.vmap[set][level - 1];
+    const float4 a = s[(size_t)(2 * y) * pw + 2 * x], b = s[(size_t)(2 * y) * pw + 2 * x + 1];
+    const float4 c = s[(size_t)(2 * y + 1) * pw + 2 * x], d = s[(size_t)(2 * y + 1) * pw + 2 * x + 1];
+    sv.vmap[set][level][i] = make_float4((((a.x + b.x) + c.x) + d.x) * 0.25f, (((a.y + b.y) + c.y) + d.y) * 0.25f,
+                                         (((a.z + b.z) + c.z) + d.z) * 0.25f, (((a.w + b.w) + c.w) + d.w) * 0.25f);
+}
+
+// computeNMapK (cuda_imgproc.cu:276-294) over every level of the reference set
+__global__ void nmap_all_kernel(const SessionView *svs) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active) return;
+    int b = blockIdx.x, level = 0;
+    for (; level < sv.levels; ++level) {
+        const int n = (sv.lv[level].w * sv.lv[level].h + blockDim.x - 1) / blockDim.x;
+        if (b < n) break;
+        b -= n;
+    }
+    if (level >= sv.levels) return;
+    const int w = sv.lv[level].w, h = sv.lv[level].h;
+    const int i = b * blockDim.x + threadIdx.x;
+    if (i >= w * h) return;
+    const int x = i % w, y = i / w;
+    const int set = sv.ts->idx;
+    const float4 *V = sv.vmap[set][level];
+    const float qnan = __int_as_float(0x7fffffff);
+    if (x < w - 1 && y < h - 1) {
+        const int x10 = max(x - 1, 0), y10 = max(y - 1, 0);
+        const float4 v00 = V[(size_t)y * w + x10], v01 = V[(size_t)y * w + x + 1];
+        const float4 v10 = V[(size_t)y10 * w + x], v11 = V[(size_t)(y + 1) * w + x];
+        const float3 a = make_float3(v01.x - v00.x, v01.y - v00.y, v01.z - v00.z);
+        const float3 bb = make_float3(v11.x - v10.x, v11.y - v10.y, v11.z - v10.z);
+        const float3 n = cross3(a, bb);
+        const float l = norm3(n.x, n.y, n.z);
+        sv.nmap[set][level][i] = make_float4(n.x / l, n.y / l, n.z / l, 1.f);
+    } else {
+        sv.nmap[set][level][i] = make_float4(qnan, qnan, qnan, qnan);
+    }
+}
+
+}  // namespace
+
+void launch_zrange(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {
+    const int cells = (ex.w / 8) * (ex.h / 8);
+    zr_init_kernel<<<dim3((cells + 255) / 256, nslots), 256, 0, st>>>(d_sv);
+    const int gz = min(max((ex.max_pool + 255) / 256, 1), 304);
+    zrange_kernel<<<dim3(gz, nslots), 256, 0, st>>>(d_sv);
+}
+
+void launch_march(const SessionView *d_sv, int nslots, const Extent &ex, float4 *vmap_ext, long long vmap_pitch,
+                  const int *layouts, cudaStream_t st) {
+    const int tiles = ((ex.w + kRayTileW - 1) / kRayTileW) * ((ex.h + kRayTileH - 1) / kRayTileH);
+    if (layouts[GBF_VOXEL_REF])
+        raycast_kernel<GBF_VOXEL_REF><<<dim3(tiles, nslots), kRayTileW * kRayTileH, 0, st>>>(d_sv, vmap_ext, vmap_pitch);
+    if (layouts[GBF_VOXEL_HALF])
+        raycast_kernel<GBF_VOXEL_HALF><<<dim3(tiles, nslots), kRayTileW * kRayTileH, 0, st>>>(d_sv, vmap_ext, vmap_pitch);
+}
+
+void launch_post(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {
+    int w = ex.w, h = ex.h, total = (w * h + 255) / 256;
+    for (int l = 1; l < ex.levels; ++l) {
+        w /= 2; h /= 2;
+        vmap_down_kernel<<<dim3((w * h + 255) / 256, nslots), 256, 0, st>>>(d_sv, l);
+        total += (w * h + 255) / 256;
+    }
+    nmap_all_kernel<<<dim3(total, nslots), 256, 0, st>>>(d_sv);
+}
+
+void launch_raycast(const SessionView *d_sv, int nslots, const Extent &ex, float4 *vmap_ext, long long vmap_pitch,
+                    int post_pyramid, const int *layouts, cudaStream_t st) {
+    launch_zrange(d_sv, nslots, ex, st);
+    launch_march(d_sv, nslots, ex, vmap_ext, vmap_pitch, layouts, st);
+    if (post_pyramid) launch_post(d_sv, nslots, ex, st);
+}
+
+}  // namespace gbf

@@ -1,0 +1,468 @@
+// tracking.cu -- fused point-to-plane ICP + photometric normal equations and
+// the device-side Gauss-Newton step (src/tracking/pose_estimator.cu:166-307,
+// src/tracking/m_estimator.cu:313-482, include/tracking/reduce_sum.h:11-61,
+// src/tracking/icp_tracker.cpp:23-156).
+//
+// GB300 design: one launch per (level, iteration) for all sessions of a batch.
+// Each CTA reduces its pixels' ICP row and photometric row (the reference runs
+// two kernels, each re-reading the reference vertex map) into 29 + 29 FP32
+// sums (warp shuffle tree, then a fixed-order shared-memory pass), writes one
+// partial record, and the last CTA of the session (atomic ticket) adds the
+// partials in FP64 in CTA order and runs the step on the device: FP64 LDL^T
+// solve of the 6x6 system, SE(3) exponential, pose composition, and the
+// reference's error-increase / revert / break rules.  No host round trip: the
+// reference pays two device->host syncs per iteration (pose_estimator.cu:302-304,
+// m_estimator.cu:477-479).  The order of every sum is fixed, so a session's
+// result does not depend on the other sessions in the batch.
+#include <float.h>
+
+#include "gbf_device.cuh"
+#include "gbf_kernels.h"
+
+namespace gbf {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// FP64 6x6 LDL^T with symmetric diagonal pivoting (the documented method of
+// Eigen::LDLT used at icp_tracker.cpp:92); zero pivots act as a pseudo-inverse.
+__device__ void ldlt_solve6(double A[6][6], const double b[6], double x[6]) {
+    int perm[6] = {0, 1, 2, 3, 4, 5};
+    double D[6];
+    for (int k = 0; k < 6; ++k) {
+        int p = k;
+        double best = fabs(A[k][k]);
+        for (int i = k + 1; i < 6; ++i)
+            if (fabs(A[i][i]) > best) { best = fabs(A[i][i]); p = i; }
+        if (p != k) {
+            for (int j = 0; j < 6; ++j) { double t = A[k][j]; A[k][j] = A[p][j]; A[p][j] = t; }
+            for (int i = 0; i < 6; ++i) { double t = A[i][k]; A[i][k] = A[i][p]; A[i][p] = t; }
+            int t = perm[k]; perm[k] = perm[p]; perm[p] = t;
+        }
+        D[k] = A[k][k];
+        if (fabs(D[k]) <= DBL_MIN) {
+            for (int i = k + 1; i < 6; ++i) A[i][k] = 0.0;
+            continue;
+        }
+        for (int i = k + 1; i < 6; ++i) {
+            const double t = A[i][k];
+            A[i][k] = t / D[k];
+            for (int j = k + 1; j <= i; ++j) A[i][j] -= A[i][k] * A[j][k] * D[k];
+            // keep the upper triangle symmetric for the next pivot search / swaps
+            for (int j = k + 1; j <= i; ++j) A[j][i] = A[i][j];
+        }
+    }
+    double z[6];
+    for (int i = 0; i < 6; ++i) z[i] = b[perm[i]];
+    for (int i = 0; i < 6; ++i)
+        for (int k = 0; k < i; ++k) z[i] -= A[i][k] * z[k];
+    for (int i = 0; i < 6; ++i) z[i] = (fabs(D[i]) > DBL_MIN) ? z[i] / D[i] : 0.0;
+    for (int i = 5; i >= 0; --i)
+        for (int k = i + 1; k < 6; ++k) z[i] -= A[k][i] * z[k];
+    for (int i = 0; i < 6; ++i) x[perm[i]] = z[i];
+}
+
+// SE(3) exponential of xi = (rho, phi), translation first (Sophus convention).
+__device__ void se3_exp(const double xi[6], double T[12]) {
+    const double wx = xi[3], wy = xi[4], wz = xi[5];
+    const double th2 = wx * wx + wy * wy + wz * wz;
+    const double th = sqrt(th2);
+    double A, B, C;
+    if (th < 1e-5) {
+        A = 1.0 - th2 / 6.0;
+        B = 0.5 - th2 / 24.0;
+        C = 1.0 / 6.0 - th2 / 120.0;
+    } else {
+        const double s = sin(th), c = cos(th);
+        A = s / th;
+        B = (1.0 - c) / th2;
+        C = (th - s) / (th2 * th);
+    }
+    const double W[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
+    double W2[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) W2[i * 3 + j] = W[i * 3] * W[j] + W[i * 3 + 1] * W[3 + j] + W[i * 3 + 2] * W[6 + j];
+    double V[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const double I = (i == j) ? 1.0 : 0.0;
+            T[i * 4 + j] = I + A * W[i * 3 + j] + B * W2[i * 3 + j];
+            V[i * 3 + j] = I + B * W[i * 3 + j] + C * W2[i * 3 + j];
+        }
+    for (int i = 0; i < 3; ++i) T[i * 4 + 3] = V[i * 3] * xi[0] + V[i * 3 + 1] * xi[1] + V[i * 3 + 2] * xi[2];
+}
+
+// |log(T)| of an SE(3) element (the success test, icp_tracker.cpp:145)
+__device__ double se3_log_norm(const double T[12]) {
+    const double tr = T[0] + T[5] + T[10];
+    double c = (tr - 1.0) * 0.5;
+    c = c > 1.0 ? 1.0 : (c < -1.0 ? -1.0 : c);
+    const double th = acos(c);
+    const double vx = T[9] - T[6], vy = T[2] - T[8], vz = T[4] - T[1];
+    double k = 0.5;
+    const double s = sin(th);
+    if (th > 1e-8 && s > 1e-12) k = th / (2.0 * s);
+    const double wx = k * vx, wy = k * vy, wz = k * vz;
+    // rho = V^-1 t,  V^-1 = I - W/2 + (1/th^2)(1 - A/(2B)) W^2
+    const double th2 = wx * wx + wy * wy + wz * wz;
+    double f;
+    if (th2 < 1e-10) {
+        f = 1.0 / 12.0;
+    } else {
+        const double t = sqrt(th2);
+        const double A = sin(t) / t, B = (1.0 - cos(t)) / th2;
+        f = (1.0 - A / (2.0 * B)) / th2;
+    }
+    const double W[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
+    const double t3[3] = {T[3], T[7], T[11]};
+    double rho[3];
+    for (int i = 0; i < 3; ++i) {
+        double r = t3[i];
+        for (int j = 0; j < 3; ++j) {
+            double w2 = W[i * 3] * W[j] + W[i * 3 + 1] * W[3 + j] + W[i * 3 + 2] * W[6 + j];
+            r += -0.5 * W[i * 3 + j] * t3[j] + f * w2 * t3[j];
+        }
+        rho[i] = r;
+    }
+    return sqrt(rho[0] * rho[0] + rho[1] * rho[1] + rho[2] * rho[2] + th2);
+}
+
+__device__ __forceinline__ bool finite_pose(const double *T) {
+    for (int i = 0; i < 12; ++i)
+        if (!isfinite(T[i])) return false;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// per-pixel rows
+__device__ __forceinline__ float interp2(const float *img, int w, float x, float y) {
+    const int u = (int)floorf(x), v = (int)floorf(y);
+    const float ax = x - (float)u, ay = y - (float)v;
+    const float *r0 = img + (size_t)v * w, *r1 = r0 + w;
+    return (r0[u] * (1.0f - ax) + r0[u + 1] * ax) * (1.0f - ay) + (r1[u] * (1.0f - ax) + r1[u + 1] * ax) * ay;
+}
+
+// ICPReduction::searchPoint + getRow (pose_estimator.cu:168-222)
+__device__ __forceinline__ bool icp_row(const SessionView &sv, int level, int rs, int cs, const M34 &T, int p,
+                                        float row[7]) {
+    const LevelK &K = sv.lv[level];
+    const float4 vl = sv.vmap[rs][level][p];
+    if (isnan(vl.x)) return false;
+    const float3 vg = T.apply(vl.x, vl.y, vl.z);
+    const float invz = (float)(1.0 / (double)vg.z);
+    const int u = __float2int_rd(((vg.x * invz) * K.fx + K.cx) + 0.5f);
+    const int v = __float2int_rd(((vg.y * invz) * K.fy + K.cy) + 0.5f);
+    if (u < 0 || v < 0 || u >= K.w || v >= K.h) return false;
+    const int q = v * K.w + u;
+    const float4 vc4 = sv.vmap[cs][level][q];
+    const float4 nl4 = sv.nmap[rs][level][p];
+    const float3 ng = T.rotate(nl4.x, nl4.y, nl4.z);
+    const float4 nc4 = sv.nmap[cs][level][q];
+    const float dist = norm3(vg.x - vc4.x, vg.y - vc4.y, vg.z - vc4.z);
+    const float3 cr = cross3(make_float3(nc4.x, nc4.y, nc4.z), ng);
+    const float sine = norm3(cr.x, cr.y, cr.z);
+    if (!(sine < sv.icp_angle && dist <= sv.icp_dist && !isnan(nc4.x) && !isnan(ng.x))) return false;
+    const float3 vxn = cross3(vg, ng);
+    row[0] = ng.x; row[1] = ng.y; row[2] = ng.z;
+    row[3] = vxn.x; row[4] = vxn.y; row[5] = vxn.z;
+    row[6] = dot3(ng, make_float3(vc4.x - vg.x, vc4.y - vg.y, vc4.z - vg.z));
+    return true;
+}
+
+// RgbReduction2::find_corresp + compute_jacobian (m_estimator.cu:315-391)
+__device__ __forceinline__ bool rgb_row(const SessionView &sv, int level, int rs, int cs, const M34 &T, float stddev,
+                                        int p, float row[7]) {
+    const LevelK &K = sv.lv[level];
+    const float4 pt = sv.vmap[rs][level][p];
+    if (pt.w < 0 || isnan(pt.x)) return false;
+    const float il = sv.inten[rs][level][p];
+    if (!isfinite(il)) return false;
+    const float3 q = T.apply(pt.x, pt.y, pt.z);
+    const float u0 = (q.x / q.z) * K.fx + K.cx;
+    const float v0 = (q.y / q.z) * K.fy + K.cy;
+    if (!(u0 >= 2 && u0 < (float)(K.w - 2) && v0 >= 2 && v0 < (float)(K.h - 2))) return false;
+    const float ic = interp2(sv.inten[cs][level], K.w, u0, v0);
+    const float dx = interp2(sv.gx[level], K.w, u0, v0);
+    const float dy = interp2(sv.gy[level], K.w, u0, v0);
+    if (!((dx > 2 || dy > 2) && isfinite(ic) && isfinite(dx) && isfinite(dy))) return false;
+    const float zi = (float)(1.0 / (double)q.z);
+    const float lx = (dx * K.fx) * zi, ly = (dy * K.fy) * zi;
+    const float lz = (-(lx * q.x + ly * q.y)) * zi;
+    float res = ic - il;
+    if ((double)stddev > 10e-5) res /= stddev;
+    const float huber = (float)(1.345 * (double)stddev);
+    float w = 1.f;
+    if (fabsf(res) > huber && (double)stddev > 10e-6) w = sqrtf(huber / fabsf(res));
+    const float3 pl = cross3(q, make_float3(lx, ly, lz));
+    row[0] = lx * w; row[1] = ly * w; row[2] = lz * w;
+    row[3] = pl.x * w; row[4] = pl.y * w; row[5] = pl.z * w;
+    row[6] = w * (-res);
+    return true;
+}
+
+__device__ __forceinline__ void accumulate(float *acc, const float row[7]) {
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < 7; ++i)
+#pragma unroll
+        for (int j = i; j < 7; ++j) acc[k++] += row[i] * row[j];
+    acc[28] += 1.0f;
+}
+
+struct ReduceArgs {
+    int level, iter, once;
+    float pose[12];
+    float stddev;
+};
+
+__device__ void gn_epilogue(const SessionView &sv, int level, int iter, const double *s);
+
+__global__ void __launch_bounds__(kReduceThreads) gn_reduce_kernel(const SessionView *svs, ReduceArgs a) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active) return;
+    TrackState *ts = sv.ts;
+    const int level = a.level;
+    if (level >= sv.levels || blockIdx.x >= sv.red_ctas[level]) return;
+    if (!a.once) {
+        if (!ts->tracking || a.iter >= sv.max_iter[level]) return;
+        if (a.iter > 0 && ts->level_done) return;
+    }
+    __shared__ M34 T;
+    __shared__ float stddev_s;
+    if (threadIdx.x == 0) {
+        if (a.once) {
+#pragma unroll
+            for (int i = 0; i < 12; ++i) T.m[i] = a.pose[i];
+            stddev_s = a.stddev;
+        } else {
+            T = pose_to_float(ts->est);
+            stddev_s = (a.iter == 0) ? 0.f : ts->stddev;
+        }
+    }
+    __syncthreads();
+    const int rs = ts->idx, cs = 1 - ts->idx;
+    const int P = sv.lv[level].w * sv.lv[level].h;
+    const float stddev = stddev_s;
+
+    float acc[kReduceWidth];
+#pragma unroll
+    for (int k = 0; k < kReduceWidth; ++k) acc[k] = 0.f;
+    const int stride = sv.red_ctas[level] * kReduceThreads;
+    for (int p = blockIdx.x * kReduceThreads + threadIdx.x; p < P; p += stride) {
+        float row[7];
+        if (icp_row(sv, level, rs, cs, T, p, row)) accumulate(acc, row);
+        if (rgb_row(sv, level, rs, cs, T, stddev, p, row)) accumulate(acc + 29, row);
+    }
+    // BlockReduce (reduce_sum.h:11-46): warp shuffle tree, then across warps
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < kReduceWidth; ++k) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
+    __shared__ float warp_sums[kReduceThreads / 32][kReduceWidth];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < kReduceWidth; ++k) warp_sums[wid][k] = acc[k];
+    __syncthreads();
+    float *part = sv.partials + (size_t)blockIdx.x * kPartialStride;
+    if (threadIdx.x < kReduceWidth) {
+        float s = 0.f;
+#pragma unroll
+        for (int w = 0; w < kReduceThreads / 32; ++w) s += warp_sums[w][threadIdx.x];
+        part[threadIdx.x] = s;
+    }
+    // last CTA of this session finishes the reduction and takes the step
+    __threadfence();
+    __syncthreads();
+    __shared__ unsigned int ticket;
+    if (threadIdx.x == 0) ticket = atomicAdd(reinterpret_cast<unsigned *>(sv.ctr + C_TICKET), 1u);
+    __syncthreads();
+    if (ticket != (unsigned)sv.red_ctas[level] - 1u) return;
+    __threadfence();
+    __shared__ double total[kReduceWidth];
+    if (threadIdx.x < kReduceWidth) {
+        double s = 0.0;
+        for (int c = 0; c < sv.red_ctas[level]; ++c) s += (double)__ldcg(sv.partials + (size_t)c * kPartialStride + threadIdx.x);
+        total[threadIdx.x] = s;
+        ts->last_sums[threadIdx.x] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        sv.ctr[C_TICKET] = 0;
+        if (!a.once) gn_epilogue(sv, level, a.iter, total);
+    }
+}
+
+// Host loop body of DenseTracking::compute_transform (icp_tracker.cpp:52-139).
+__device__ void gn_epilogue(const SessionView &sv, int level, int iter, const double *s) {
+    TrackState *ts = sv.ts;
+    // create_jtjjtr (reduce_sum.h:48-61): float matrices from the sums
+    float Hi[6][6], Hr[6][6], bi[6], br[6];
+    int k = 0;
+    for (int i = 0; i < 6; ++i)
+        for (int j = i; j < 7; ++j, ++k) {
+            const float vi = (float)s[k], vr = (float)s[29 + k];
+            if (j == 6) {
+                bi[i] = vi; br[i] = vr;
+            } else {
+                Hi[i][j] = Hi[j][i] = vi;
+                Hr[i][j] = Hr[j][i] = vr;
+            }
+        }
+    const float r_icp = (float)s[27], n_icp = (float)s[28];
+    const float r_rgb = (float)s[29 + 27], n_rgb = (float)s[29 + 28];
+    const float stddev_next = sqrtf(r_rgb / (n_rgb - 6.0f));
+    double A[6][6], b[6], xi[6];
+    for (int i = 0; i < 6; ++i) {
+        for (int j = 0; j < 6; ++j) A[i][j] = (double)(sv.w_icp * Hi[i][j] + sv.w_rgb * Hr[i][j]);
+        b[i] = (double)(sv.w_icp * bi[i] + sv.w_rgb * br[i]);
+    }
+    ldlt_solve6(A, b, xi);
+    double E[12], next[12];
+    se3_exp(xi, E);
+    pose_mul(E, ts->est, next);
+    pose_copy(ts->est, ts->est_prev);
+    pose_copy(next, ts->est);
+    ts->iterations += 1;
+    ts->icp_inliers = n_icp;
+    ts->rgb_inliers = n_rgb;
+
+    const float last_icp = (iter == 0) ? FLT_MAX : ts->icp_error;
+    const float last_rgb = (iter == 0) ? FLT_MAX : ts->rgb_error;
+    int icp_count = (iter == 0) ? 0 : ts->icp_count;
+    int rgb_count = (iter == 0) ? 0 : ts->rgb_count;
+    ts->level_done = 0;
+    ts->stddev = stddev_next;
+    float icp_error = sqrtf(r_icp) / n_icp;
+    if (isnan(icp_error)) {
+        ts->invalid = 1;
+        ts->level_done = 1;
+        ts->icp_error = icp_error;
+        return;
+    }
+    if (icp_error > last_icp) {
+        if (icp_count >= 2) {
+            pose_copy(ts->est_prev, ts->est);
+            ts->level_done = 1;
+            return;
+        }
+        icp_count++;
+        icp_error = last_icp;
+    } else {
+        icp_count = 0;
+    }
+    ts->icp_error = icp_error;
+    ts->icp_count = icp_count;
+    float rgb_error = sqrtf(r_rgb) / n_rgb;
+    if (isnan(rgb_error)) {
+        ts->invalid = 1;
+        ts->level_done = 1;
+        ts->rgb_error = rgb_error;
+        return;
+    }
+    if (rgb_error > last_rgb) {
+        if (rgb_count >= 2) {
+            pose_copy(ts->est_prev, ts->est);
+            ts->level_done = 1;
+            return;
+        }
+        rgb_count++;
+        rgb_error = last_rgb;
+    } else {
+        rgb_count = 0;
+    }
+    ts->rgb_error = rgb_error;
+    ts->rgb_count = rgb_count;
+}
+
+// frame_mode 1: System frame (track only when a reference exists); 0: gbf_track.
+__global__ void track_begin_kernel(const SessionView *svs, int frame_mode) {
+    const SessionView &sv = svs[blockIdx.x];
+    if (!sv.active || threadIdx.x != 0) return;
+    TrackState *ts = sv.ts;
+    ts->tracking = frame_mode ? ts->has_ref : 1;
+    // Revertable(initial_estimate): curr = init, prev = identity
+    pose_copy(ts->init, ts->est);
+    pose_identity(ts->est_prev);
+    ts->invalid = 0;
+    ts->iterations = 0;
+    ts->level_done = 0;
+    ts->icp_error = FLT_MAX;
+    ts->rgb_error = FLT_MAX;
+    ts->stddev = 0.f;
+    ts->icp_count = ts->rgb_count = 0;
+    sv.ctr[C_TICKET] = 0;
+}
+
+// Tracking result (icp_tracker.cpp:143-155); frame_mode 1 also applies the
+// System / DenseOdometry bookkeeping (rgbd_odometry.cpp:39-41): pose update
+// and reference swap.
+__global__ void track_finish_kernel(const SessionView *svs, int frame_mode) {
+    const SessionView &sv = svs[blockIdx.x];
+    if (!sv.active || threadIdx.x != 0) return;
+    TrackState *ts = sv.ts;
+    if (ts->tracking) {
+        double inv[12], rel[12];
+        pose_inverse(ts->est, inv);
+        pose_mul(inv, ts->init, rel);
+        const double n = se3_log_norm(rel);
+        const bool finite = finite_pose(ts->est);
+        const bool fail = ts->invalid || !(n <= 0.1) || !finite;
+        if (!finite) raise_flag(sv, GBF_FLAG_NAN_POSE);
+        if (fail) {
+            pose_identity(ts->update);
+            ts->success = 0;
+        } else {
+            pose_copy(inv, ts->update);
+            ts->success = 1;
+        }
+        if (frame_mode) {
+            double np[12];
+            pose_mul(ts->pose, ts->update, np);
+            pose_copy(np, ts->pose);
+            if (fail) raise_flag(sv, GBF_FLAG_TRACK_FAILED);
+        }
+    } else if (frame_mode) {
+        ts->success = 1;
+        pose_identity(ts->update);
+    }
+    if (frame_mode) {
+        ts->idx = 1 - ts->idx;
+        ts->has_ref = 1;
+        pose_copy(ts->pose, ts->map_pose);
+        ts->frame_index += 1;
+    }
+}
+
+}  // namespace
+
+void launch_track(const SessionView *d_sv, int nslots, const Extent &ex, int frame_mode, cudaStream_t st) {
+    track_begin_kernel<<<nslots, 32, 0, st>>>(d_sv, frame_mode);
+    ReduceArgs a{};
+    a.once = 0;
+    for (int level = ex.levels - 1; level >= 0; --level) {
+        for (int iter = 0; iter < ex.max_iter[level]; ++iter) {
+            a.level = level;
+            a.iter = iter;
+            gn_reduce_kernel<<<dim3(ex.max_red[level], nslots), kReduceThreads, 0, st>>>(d_sv, a);
+        }
+    }
+    track_finish_kernel<<<nslots, 32, 0, st>>>(d_sv, frame_mode);
+}
+
+void launch_reduce_once(const SessionView *d_sv, const Extent &ex, int level, const float *pose12, float stddev,
+                        cudaStream_t st) {
+    ReduceArgs a{};
+    a.once = 1;
+    a.level = level;
+    a.iter = 0;
+    for (int i = 0; i < 12; ++i) a.pose[i] = pose12[i];
+    a.stddev = stddev;
+    gn_reduce_kernel<<<dim3(ex.max_red[level], 1), kReduceThreads, 0, st>>>(d_sv, a);
+}
+
+void launch_frame_finish(const SessionView *d_sv, int nslots, cudaStream_t st) {
+    track_finish_kernel<<<nslots, 32, 0, st>>>(d_sv, 1);
+}
+
+}  // namespace gbf

@@ -1,0 +1,287 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, always as the checker, never as the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liboracle.so"
+MAX_LEVELS = 5
+
+
+class OrConfig(C.Structure):
+    _fields_ = [
+        ("voxel_size", C.c_float), ("truncation", C.c_float),
+        ("zmin_update", C.c_float), ("zmax_update", C.c_float),
+        ("zmin_raycast", C.c_float), ("zmax_raycast", C.c_float),
+        ("num_blocks", C.c_int32), ("voxel_layout", C.c_int32), ("num_levels", C.c_int32),
+        ("max_iterations", C.c_int32 * MAX_LEVELS),
+        ("w_icp", C.c_float), ("w_rgb", C.c_float), ("icp_dist_thresh", C.c_float),
+        ("icp_angle_thresh", C.c_float), ("bilateral", C.c_int32), ("threads", C.c_int32),
+    ]
+
+
+class OrIntrinsics(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float)]
+
+
+class OrTrackResult(C.Structure):
+    _fields_ = [("success", C.c_int32), ("iterations", C.c_int32), ("icp_error", C.c_float),
+                ("rgb_error", C.c_float), ("icp_inliers", C.c_float), ("rgb_inliers", C.c_float),
+                ("update", C.c_double * 16)]
+
+
+def build() -> Path:
+    """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        L = C.CDLL(str(LIB_PATH))
+        P, D = C.c_void_p, C.POINTER(C.c_double)
+        for s in ("f32", "f64"):
+            sig = {
+                f"or_map_create_{s}": (P, [C.POINTER(OrConfig), C.POINTER(OrIntrinsics)]),
+                f"or_map_destroy_{s}": (None, [P]),
+                f"or_fuse_{s}": (C.c_int, [P, P, P, P, D]),
+                f"or_raycast_{s}": (C.c_int, [P, D, P]),
+                f"or_map_blocks_{s}": (C.c_int64, [P]),
+                f"or_map_export_{s}": (C.c_int64, [P, P, P, P, P, C.c_int64]),
+                f"or_visible_{s}": (C.c_int64, [P, P, C.c_int64]),
+                f"or_zrange_{s}": (None, [P, P]),
+                f"or_render_blocks_{s}": (C.c_int32, [P]),
+                f"or_mesh_{s}": (C.c_int64, [P, C.c_int, P, P, C.c_int64]),
+                f"or_frame_create_{s}": (P, [C.POINTER(OrConfig), C.POINTER(OrIntrinsics)]),
+                f"or_frame_destroy_{s}": (None, [P]),
+                f"or_build_pyramid_{s}": (None, [P, P, P]),
+                f"or_frame_get_{s}": (None, [P, C.c_int, C.c_int, P]),
+                f"or_frame_set_vmap_{s}": (None, [P, P]),
+                f"or_reduce_{s}": (None, [P, P, C.c_int, C.POINTER(C.c_float), C.c_float, D]),
+                f"or_track_{s}": (None, [P, P, D, C.POINTER(OrTrackResult)]),
+                f"or_system_create_{s}": (P, [C.POINTER(OrConfig), C.POINTER(OrIntrinsics)]),
+                f"or_system_destroy_{s}": (None, [P]),
+                f"or_system_set_pose_{s}": (None, [P, D]),
+                f"or_system_get_pose_{s}": (None, [P, D]),
+                f"or_process_frame_{s}": (None, [P, P, P]),
+                f"or_system_map_{s}": (P, [P]),
+                f"or_system_ref_{s}": (P, [P]),
+                f"or_system_last_result_{s}": (None, [P, C.POINTER(OrTrackResult)]),
+            }
+            for name, (res, args) in sig.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+        L.or_compute_hash.restype = C.c_int
+        L.or_compute_hash.argtypes = [C.c_int] * 4
+        L.or_floor_ref.restype = C.c_int
+        L.or_floor_ref.argtypes = [C.c_float]
+        L.or_voxel_to_block.argtypes = [P, P]
+        L.or_voxel_to_local.argtypes = [P, P]
+        L.or_local_idx.restype = C.c_int
+        L.or_local_idx.argtypes = [P]
+        L.or_tri_table.restype = C.c_int
+        L.or_tri_table.argtypes = [C.c_int, P]
+        L.or_edge_table.restype = C.c_int
+        L.or_edge_table.argtypes = [C.c_int]
+        L.or_pack_sdf.restype = C.c_short
+        L.or_pack_sdf.argtypes = [C.c_float]
+        L.or_unpack_sdf.restype = C.c_float
+        L.or_unpack_sdf.argtypes = [C.c_short]
+        _lib = L
+    return _lib
+
+
+def config_from(gcfg, threads: int = 0) -> OrConfig:
+    """Oracle config from a libgbfusion Config (same field meanings)."""
+    c = OrConfig()
+    for f, _ in OrConfig._fields_:
+        if f == "threads":
+            continue
+        if f == "max_iterations":
+            for i in range(MAX_LEVELS):
+                c.max_iterations[i] = gcfg.max_iterations[i]
+        else:
+            setattr(c, f, getattr(gcfg, f))
+    c.threads = threads
+    return c
+
+
+def intrinsics_from(K) -> OrIntrinsics:
+    return OrIntrinsics(K.width, K.height, K.fx, K.fy, K.cx, K.cy)
+
+
+def _d16(T):
+    a = np.ascontiguousarray(np.asarray(T, np.float64).reshape(16))
+    return (C.c_double * 16)(*a.tolist())
+
+
+def _p(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+class OracleMap:
+    def __init__(self, cfg: OrConfig, K: OrIntrinsics, precision: str = "f32"):
+        self.s = precision
+        self.cfg, self.K = cfg, K
+        self.h = getattr(lib(), f"or_map_create_{precision}")(C.byref(cfg), C.byref(K))
+
+    def fn(self, name):
+        return getattr(lib(), f"{name}_{self.s}")
+
+    def fuse(self, depth: np.ndarray, rgb: np.ndarray, pose, nmap: np.ndarray | None = None) -> int:
+        depth = np.ascontiguousarray(depth, np.float32)
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        nmap = None if nmap is None else np.ascontiguousarray(nmap, np.float32)
+        return self.fn("or_fuse")(self.h, _p(depth), _p(rgb), _p(nmap), _d16(pose))
+
+    def raycast(self, pose, vmap: np.ndarray | None = None) -> np.ndarray:
+        if vmap is None:
+            vmap = np.full((self.K.height, self.K.width, 4), np.nan, np.float32)
+        self.fn("or_raycast")(self.h, _d16(pose), _p(vmap))
+        return vmap
+
+    def export(self):
+        n = self.fn("or_map_blocks")(self.h)
+        coords = np.zeros((n, 3), np.int32)
+        sdf = np.zeros((n, 512), np.float32)
+        w = np.zeros((n, 512), np.float32)
+        rgb = np.zeros((n, 512, 3), np.uint8)
+        self.fn("or_map_export")(self.h, _p(coords), _p(sdf), _p(w), _p(rgb), n)
+        return coords, sdf, w, rgb
+
+    def visible(self) -> np.ndarray:
+        n = self.fn("or_visible")(self.h, None, 0)
+        out = np.zeros((n, 3), np.int32)
+        self.fn("or_visible")(self.h, _p(out), n)
+        return out
+
+    def zrange(self) -> np.ndarray:
+        out = np.zeros((self.K.height // 8, self.K.width // 8, 2), np.float32)
+        self.fn("or_zrange")(self.h, _p(out))
+        return out
+
+    def render_blocks(self) -> int:
+        return self.fn("or_render_blocks")(self.h)
+
+    def mesh(self, mode: int, max_tris: int = 1 << 22):
+        vtx = np.zeros((max_tris, 3, 3), np.float32)
+        attr = None
+        if mode == 1:
+            attr = np.zeros((max_tris, 3, 3), np.float32)
+        elif mode == 2:
+            attr = np.zeros((max_tris, 3, 3), np.uint8)
+        n = self.fn("or_mesh")(self.h, mode, _p(vtx), _p(attr), max_tris)
+        n = min(n, max_tris)
+        return vtx[:n], (attr[:n] if attr is not None else None)
+
+    def __del__(self):
+        try:
+            self.fn("or_map_destroy")(self.h)
+        except Exception:
+            pass
+
+
+class OracleFrame:
+    def __init__(self, cfg: OrConfig, K: OrIntrinsics, precision: str = "f32", handle=None, owner=None):
+        self.s, self.cfg, self.K = precision, cfg, K
+        self._own = handle is None
+        self._owner = owner
+        self.h = getattr(lib(), f"or_frame_create_{precision}")(C.byref(cfg), C.byref(K)) if handle is None else handle
+
+    def fn(self, name):
+        return getattr(lib(), f"{name}_{self.s}")
+
+    def build(self, depth_m: np.ndarray, rgb: np.ndarray) -> None:
+        depth_m = np.ascontiguousarray(depth_m, np.float32)
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        self.fn("or_build_pyramid")(self.h, _p(depth_m), _p(rgb))
+
+    def get(self, kind: int, level: int) -> np.ndarray:
+        w, h = self.K.width >> level, self.K.height >> level
+        out = np.zeros((h, w, 4) if kind in (0, 1) else (h, w), np.float32)
+        self.fn("or_frame_get")(self.h, kind, level, _p(out))
+        return out
+
+    def set_vmap(self, vmap0: np.ndarray) -> None:
+        self.fn("or_frame_set_vmap")(self.h, _p(np.ascontiguousarray(vmap0, np.float32)))
+
+    def __del__(self):
+        if self._own:
+            try:
+                self.fn("or_frame_destroy")(self.h)
+            except Exception:
+                pass
+
+
+def reduce(ref: OracleFrame, cur: OracleFrame, level: int, T, stddev: float = 0.0) -> np.ndarray:
+    Tf = (C.c_float * 12)(*np.asarray(T, np.float64).reshape(-1)[:12].astype(np.float32).tolist())
+    out = (C.c_double * 58)()
+    getattr(lib(), f"or_reduce_{ref.s}")(ref.h, cur.h, level, Tf, stddev, out)
+    return np.array(out[:])
+
+
+def track(ref: OracleFrame, cur: OracleFrame, init=None):
+    r = OrTrackResult()
+    getattr(lib(), f"or_track_{ref.s}")(ref.h, cur.h, _d16(np.eye(4) if init is None else init), C.byref(r))
+    return r
+
+
+class OracleSystem:
+    def __init__(self, cfg: OrConfig, K: OrIntrinsics, precision: str = "f32"):
+        self.s, self.cfg, self.K = precision, cfg, K
+        self.h = getattr(lib(), f"or_system_create_{precision}")(C.byref(cfg), C.byref(K))
+
+    def fn(self, name):
+        return getattr(lib(), f"{name}_{self.s}")
+
+    def set_pose(self, T) -> None:
+        self.fn("or_system_set_pose")(self.h, _d16(T))
+
+    def pose(self) -> np.ndarray:
+        out = (C.c_double * 16)()
+        self.fn("or_system_get_pose")(self.h, out)
+        return np.array(out[:]).reshape(4, 4)
+
+    def process(self, depth_mm: np.ndarray, rgb: np.ndarray) -> None:
+        self.fn("or_process_frame")(self.h, _p(np.ascontiguousarray(depth_mm, np.uint16)),
+                                    _p(np.ascontiguousarray(rgb, np.uint8)))
+
+    def last_result(self) -> OrTrackResult:
+        r = OrTrackResult()
+        self.fn("or_system_last_result")(self.h, C.byref(r))
+        return r
+
+    def map_export(self):
+        m = OracleMap.__new__(OracleMap)
+        m.s, m.cfg, m.K = self.s, self.cfg, self.K
+        m.h = self.fn("or_system_map")(self.h)
+        out = m.export()
+        m.h = None
+        return out
+
+    def ref_frame(self) -> OracleFrame:
+        return OracleFrame(self.cfg, self.K, self.s, handle=self.fn("or_system_ref")(self.h), owner=self)
+
+    def __del__(self):
+        try:
+            self.fn("or_system_destroy")(self.h)
+        except Exception:
+            pass

@@ -1,0 +1,217 @@
+"""CUDA kernels against the FP32 oracle on identical inputs (through the C ABI).
+
+Integer / byte results (block sets, visible sets, z-range cells, hit masks,
+mesh topology) must be bit-exact.  Float results that pass through no
+transcendental function (1/d^2 colour integration, raycast, marching cubes)
+are expected bit-exact too; the normal-weighted update (sin) and the
+bilateral filter (exp) are checked within stated ulp-level tolerances.
+"""
+import numpy as np
+import pytest
+
+import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_map(L, cfg, K, precision="f32"):
+    import oracle as O
+    return O.OracleMap(O.config_from(cfg), O.intrinsics_from(K), precision)
+
+
+def _compare_maps(g, o, exact=True, sdf_tol=0.0, w_rtol=0.0, rgb_tol=0):
+    gc, gs, gw, gr = H.sort_blocks(*g)
+    oc, os_, ow, orr = H.sort_blocks(*o)
+    assert gc.shape == oc.shape and np.array_equal(gc, oc), "allocated block sets differ"
+    if exact:
+        assert np.array_equal(gs, os_) and np.array_equal(gw, ow) and np.array_equal(gr, orr)
+    else:
+        assert np.abs(gs - os_).max() <= sdf_tol
+        assert np.allclose(gw, ow, rtol=w_rtol, atol=1e-6)
+        assert np.abs(gr.astype(int) - orr.astype(int)).max() <= rgb_tol
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_fuse_colour_update_bit_exact(gbf, layout):
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, layout)
+    m = L.DenseMapping(K, cfg)
+    om = _oracle_map(L, cfg, K)
+    for d, c, T in H.frames(L, K, 4, step=5):
+        dm = H.depth_m(d)
+        m.update(H.cuda(dm), H.cuda(c), T)
+        nvis = om.fuse(dm, c, T)
+        gv, ov = H.sort_blocks(m.visible_blocks())[0], H.sort_blocks(om.visible())[0]
+        assert len(gv) == nvis and np.array_equal(gv, ov), "visible block sets differ"
+    _compare_maps(m.export(), om.export(), exact=True)
+    assert m.stats().status == 0
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_fuse_weighted_update(gbf, layout):
+    """update(RgbdImagePtr): weight |sin(n_c.z)|/d^2 -- sin rounds differently on
+    the GPU and in libm, so sdf may differ by one storage quantum."""
+    import oracle as O
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, layout)
+    m = L.DenseMapping(K, cfg)
+    om = _oracle_map(L, cfg, K)
+    fr = O.OracleFrame(O.config_from(cfg), O.intrinsics_from(K))
+    for d, c, T in H.frames(L, K, 3, step=7):
+        dm = H.depth_m(d)
+        fr.build(dm, c)
+        n0 = fr.get(1, 0)
+        m.update(H.cuda(dm), H.cuda(c), T, normal=H.cuda(n0))
+        om.fuse(dm, c, T, nmap=n0)
+    q = 2.0 / 32767 if layout == 0 else 2e-3
+    _compare_maps(m.export(), om.export(), exact=False, sdf_tol=q, w_rtol=1e-5 if layout == 0 else 1e-2, rgb_tol=1)
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_raycast_bit_exact(gbf, layout):
+    L = gbf
+    import torch
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, layout)
+    m = L.DenseMapping(K, cfg)
+    om = _oracle_map(L, cfg, K)
+    fr = H.frames(L, K, 3, step=4)
+    for d, c, T in fr:
+        dm = H.depth_m(d)
+        m.update(H.cuda(dm), H.cuda(c), T)
+        om.fuse(dm, c, T)
+    T = fr[-1][2]
+    vm = torch.full((K.height, K.width, 4), float("nan"), device="cuda")
+    m.raycast(vm, T)
+    g = vm.cpu().numpy()
+    o = om.raycast(T)
+    assert np.array_equal(m.zrange(), om.zrange()), "z-range grids differ"
+    gh, oh = ~np.isnan(g[..., 2]), ~np.isnan(o[..., 2])
+    assert np.array_equal(gh, oh), f"hit masks differ in {np.sum(gh != oh)} pixels"
+    assert gh.mean() > 0.8
+    assert np.array_equal(g[gh], o[oh])
+
+
+def test_pyramid_parity(gbf):
+    import oracle as O
+    L = gbf
+    K = H.intrinsics(L)
+    for bil in (0, 1):
+        cfg = H.small_config(L, 0, bilateral=bil)
+        t = L.DenseTracking(K, cfg)
+        fr = O.OracleFrame(O.config_from(cfg), O.intrinsics_from(K))
+        d, c, T = H.frames(L, K, 1)[0]
+        dm = H.depth_m(d)
+        t.set_reference(H.cuda(dm), H.cuda(c))
+        fr.build(dm, c)
+        for lvl in range(3):
+            for kind in range(6):
+                g = t.get_image(1, kind, lvl).cpu().numpy()
+                o = fr.get(kind, lvl)
+                if kind in (2, 3, 4) or bil == 0:
+                    assert np.array_equal(g, o, equal_nan=True), (bil, lvl, kind)
+                else:
+                    # expf differs between CUDA and libm by a few ulp
+                    fin = np.isfinite(o)
+                    assert np.array_equal(fin, np.isfinite(g)), (lvl, kind)
+                    assert np.allclose(g[fin], o[fin], rtol=2e-5, atol=2e-5), (lvl, kind)
+
+
+def _tracking_pair(L, K, cfg, a, b):
+    import oracle as O
+    t = L.DenseTracking(K, cfg)
+    (d0, c0, T0), (d1, c1, T1) = a, b
+    t.set_reference(H.cuda(H.depth_m(d0)), H.cuda(c0))
+    t.set_current(H.cuda(H.depth_m(d1)), H.cuda(c1))
+    ref = O.OracleFrame(O.config_from(cfg), O.intrinsics_from(K))
+    cur = O.OracleFrame(O.config_from(cfg), O.intrinsics_from(K))
+    ref.build(H.depth_m(d0), c0)
+    cur.build(H.depth_m(d1), c1)
+    rel = np.linalg.inv(T1) @ T0  # reference -> current
+    return t, ref, cur, rel
+
+
+def test_reduction_parity(gbf):
+    import oracle as O
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 0, bilateral=0)
+    fr = H.frames(L, K, 2, step=1)
+    t, ref, cur, rel = _tracking_pair(L, K, cfg, fr[0], fr[1])
+    for lvl in range(3):
+        for T, sd in ((np.eye(4), 0.0), (rel, 0.0), (rel, 7.5)):
+            g = t.reduce(lvl, T, sd)
+            o = O.reduce(ref, cur, lvl, T, sd)
+            assert g[28] == o[28] and g[57] == o[57], "correspondence counts differ"
+            assert g[28] > 100 and g[57] > 100
+            scale = np.maximum(np.abs(o), 1e-3 * np.abs(o).max())
+            # FP32 pairwise tree vs FP64 sequential sums
+            assert np.all(np.abs(g - o) <= 2e-5 * scale + 1e-9), (lvl, np.max(np.abs(g - o) / scale))
+
+
+def test_tracking_parity(gbf):
+    import oracle as O
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 0, bilateral=0)
+    fr = H.frames(L, K, 3, step=1)
+    t, ref, cur, rel = _tracking_pair(L, K, cfg, fr[0], fr[2])
+    g = t.compute_transform(np.eye(4))
+    o = O.track(ref, cur)
+    go = np.array(o.update[:]).reshape(4, 4)
+    assert g.sucess == bool(o.success)
+    assert abs(g.iterations - o.iterations) <= 2
+    assert np.abs(g.update[:3, 3] - go[:3, 3]).max() < 1e-4
+    assert np.abs(g.update[:3, :3] - go[:3, :3]).max() < 1e-4
+    # against ground truth: update = T_ref<-cur
+    truth = np.linalg.inv(fr[0][2]) @ fr[2][2]
+    assert np.abs(g.update[:3, 3] - truth[:3, 3]).max() < 5e-3
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_mesh_parity(gbf, mode):
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 0)
+    m = L.DenseMapping(K, cfg)
+    om = _oracle_map(L, cfg, K)
+    for d, c, T in H.frames(L, K, 3, step=6):
+        dm = H.depth_m(d)
+        m.update(H.cuda(dm), H.cuda(c), T)
+        om.fuse(dm, c, T)
+    ov, oa = om.mesh(mode, 1 << 21)
+    cap = len(ov) + 16
+    vtx = torch.zeros((cap, 3, 3), dtype=torch.float32, device="cuda")
+    if mode == 0:
+        n = m.fetch_mesh_vertex_only(vtx)
+        attr = None
+    elif mode == 1:
+        attr = torch.zeros((cap, 3, 3), dtype=torch.float32, device="cuda")
+        n = m.fetch_mesh_with_normal(vtx, attr)
+    else:
+        attr = torch.zeros((cap, 3, 3), dtype=torch.uint8, device="cuda")
+        n = m.fetch_mesh_with_colour(vtx, attr)
+    assert n == len(ov) and n > 1000
+    gv = vtx[:n].cpu().numpy()
+    if attr is None:
+        assert np.array_equal(H.sort_tris(gv)[0], H.sort_tris(ov)[0])
+    else:
+        ga = attr[:n].cpu().numpy()
+        g2 = H.sort_tris(gv, ga)
+        o2 = H.sort_tris(ov, oa)
+        assert np.array_equal(g2[0], o2[0])
+        assert np.array_equal(g2[1], o2[1])
+
+
+def test_mesh_clamps_to_capacity(gbf):
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    m = L.DenseMapping(K, H.small_config(L, 0))
+    d, c, T = H.frames(L, K, 1)[0]
+    m.update(H.cuda(H.depth_m(d)), H.cuda(c), T)
+    vtx = torch.zeros((100, 3, 3), dtype=torch.float32, device="cuda")
+    assert m.fetch_mesh_vertex_only(vtx) == 100

@@ -1,0 +1,94 @@
+"""End to end: System::process_images on the GPU against the FP32 oracle and
+the ground-truth trajectory, and the batch path against single sessions."""
+import numpy as np
+import pytest
+
+import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_gpu(L, K, cfg, fr):
+    s = L.System(K, cfg)
+    s.set_pose(fr[0][2])
+    poses = []
+    for d, c, T in fr:
+        s.process_images(H.cuda(d), H.cuda(c))
+        poses.append(s.get_camera_pose())
+    return s, poses
+
+
+def test_system_matches_oracle_and_ground_truth(gbf):
+    import oracle as O
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 0, bilateral=0)
+    fr = H.frames(L, K, 12)
+    s, gp = _run_gpu(L, K, cfg, fr)
+    osys = O.OracleSystem(O.config_from(cfg), O.intrinsics_from(K))
+    osys.set_pose(fr[0][2])
+    op = []
+    for d, c, T in fr:
+        osys.process(d, c)
+        op.append(osys.pose())
+    gp, op = np.array(gp), np.array(op)
+    truth = np.array([f[2] for f in fr])
+    # drift of the GPU path against the oracle: <= 1 mm (spec bound)
+    assert np.abs(gp[:, :3, 3] - op[:, :3, 3]).max() < 1e-3
+    assert np.abs(gp[:, :3, :3] - op[:, :3, :3]).max() < 1e-3
+    # and the tracker follows the synthetic trajectory
+    assert np.abs(gp[:, :3, 3] - truth[:, :3, 3]).max() < 0.02
+    st = s.stats()
+    assert st.status == 0 and st.frame_index == len(fr)
+    gc = H.sort_blocks(s.export()[0])[0]
+    oc = H.sort_blocks(osys.map_export()[0])[0]
+    a = {tuple(x) for x in gc}
+    b = {tuple(x) for x in oc}
+    assert len(a & b) / len(a | b) > 0.99
+
+
+def test_batch_session_isolation(gbf):
+    """A session gives the same result alone and batched with others of other
+    resolutions / voxel sizes (bit-identical pose and map)."""
+    import torch
+    L = gbf
+    KA = H.intrinsics(L, 320, 240)
+    KB = H.intrinsics(L, 160, 120)
+    cfgA = H.small_config(L, 0)
+    cfgB = H.small_config(L, 1, voxel_size=0.016, truncation=0.048)
+    frA = H.frames(L, KA, 5, seed=3)
+    frB = H.frames(L, KB, 5, seed=9)
+
+    alone = L.System(KA, cfgA)
+    alone.set_pose(frA[0][2])
+    for d, c, T in frA:
+        alone.process_images(H.cuda(d), H.cuda(c))
+    pa = alone.get_camera_pose()
+    ma = alone.export()
+
+    for use_graph in (False, True):
+        a = L.System(KA, cfgA)
+        b = L.System(KB, cfgB)
+        b2 = L.System(KB, cfgB)
+        a.set_pose(frA[0][2])
+        b.set_pose(frB[0][2])
+        b2.set_pose(frB[0][2])
+        batch = L.FusionBatch(4)
+        batch.set(0, b)
+        batch.set(2, a)
+        batch.set(3, b2)
+        for i in range(5):
+            for sess, (d, c, T) in ((a, frA[i]), (b, frB[i]), (b2, frB[i])):
+                sess.stage(H.cuda(d), H.cuda(c))
+            batch.process([True, True, True, True], use_graph=use_graph)
+            torch.cuda.synchronize()
+        assert np.array_equal(a.get_camera_pose(), pa)
+        mb = a.export()
+        for x, y in zip(ma, mb):
+            xs = H.sort_blocks(ma[0], x)[1]
+            ys = H.sort_blocks(mb[0], y)[1]
+            assert np.array_equal(xs, ys)
+        # the two identical B sessions agree with each other
+        assert np.array_equal(b.get_camera_pose(), b2.get_camera_pose())
+        batch.close()
+
