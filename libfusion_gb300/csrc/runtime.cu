@@ -254,8 +254,13 @@ gbf_status set_map_pose(gbf_session *s, const double T[16], cudaStream_t st) {
 constexpr int kPhases = 7;
 void enqueue_frame(const SessionView *d_sv, int nslots, const Extent &ex, const int *layouts, const IngestArgs &in,
                    cudaStream_t st, cudaEvent_t *ev = nullptr) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (ev) cudaStreamIsCapturing(st, &cs);
     auto mark = [&](int i) {
-        if (ev) cudaEventRecord(ev[i], st);
+        if (!ev) return;
+        // inside a capture the record must become an event-record node of the graph
+        if (cs == cudaStreamCaptureStatusActive) cudaEventRecordWithFlags(ev[i], st, cudaEventRecordExternal);
+        else cudaEventRecord(ev[i], st);
     };
     mark(0);
     launch_ingest(d_sv, nslots, ex, in, st);

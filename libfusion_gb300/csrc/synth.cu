@@ -131,7 +131,7 @@ struct SynthScene {
 static void path_at(const SynthScene &sc, int k, double pos[3], double fwd[3]) {
     const gbf_synth_params &p = sc.p;
     const double cx = p.room[0] * 0.5, cy = p.room[1] * 0.5;
-    const double jitter = p.yaw_jitter_deg * M_PI / 180.0 * sin(2.0 * M_PI * k / 37.0 + 0.7);
+    const double jitter = p.yaw_jitter_deg * M_PI / 180.0 * sin(2.0 * M_PI * k / 150.0 + 0.7);  // smooth, 5 s period
     double yaw;
     if (p.trajectory == 0) {
         const double th = 2.0 * M_PI * k / (p.frames_per_loop > 0 ? p.frames_per_loop : 200);
@@ -196,7 +196,7 @@ GBF_API gbf_status gbf_synth_default(gbf_synth_params *p) {
     d.seed = 0;
     d.trajectory = 0;
     d.radius = 1.5f; d.height = 1.4f; d.yaw_jitter_deg = 10.f; d.speed = 0.5f; d.fps = 30.f;
-    d.frames_per_loop = 200;
+    d.frames_per_loop = 600;  // 0.47 m/s at 30 fps on the 1.5 m circle
     d.noise = 1.f;
     d.zclip_min = 0.3f; d.zclip_max = 4.0f;
     *p = d;

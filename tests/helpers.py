@@ -43,6 +43,11 @@ def sort_blocks(coords, *arrays):
 
 
 def sort_tris(v, *attrs):
-    key = np.ascontiguousarray(v.reshape(len(v), 9))
-    order = np.lexsort(key.T[::-1])
+    """Canonical triangle order: by the 9 vertex coordinates, ties broken by
+    the attributes (duplicate triangles from neighbouring cubes)."""
+    cols = [v.reshape(len(v), 9)[:, i] for i in range(9)]
+    for a in attrs:
+        flat = a.reshape(len(a), -1).astype(np.float64)
+        cols += [np.nan_to_num(flat[:, i], nan=1e30) for i in range(flat.shape[1])]
+    order = np.lexsort(cols[::-1])
     return (v[order],) + tuple(a[order] for a in attrs)
