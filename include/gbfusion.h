@@ -180,6 +180,26 @@ GBF_API gbf_status gbf_build_pyramid(gbf_session *s, int32_t which, const float 
  * RGB sums in the create_jtjjtr packing (reduce_sum.h:48-61). Synchronises. */
 GBF_API gbf_status gbf_reduce(gbf_session *s, int32_t level, const double T[16], float stddev,
                               double out[58], void *stream);
+/* Level-0 images of a reference and a current frame, owned by the caller (dense
+ * rows; vertex / normal maps float4 per pixel, intensities and gradients float). */
+typedef struct gbf_reduce_inputs {
+    int32_t width, height;
+    float fx, fy, cx, cy;
+    const float *ref_vmap, *ref_nmap, *ref_intensity;
+    const float *cur_vmap, *cur_nmap, *cur_intensity, *cur_didx, *cur_didy;
+    float dist_thresh, angle_thresh;
+} gbf_reduce_inputs;
+/* No counterpart in the reference: the same 58 sums as gbf_reduce, for callers
+ * that cannot allocate device memory (inside CUDA graph capture, allocation-free
+ * real-time loops, frameworks that own all device memory).  Needs no session and
+ * calls no cudaMalloc / cudaFree: its scratch (per-CTA partials + a ticket) is a
+ * fixed 512 KB array in the library that every GPU loading the library keeps
+ * until exit.  Images up to 2,097,152 pixels (larger ones return
+ * GBF_ERR_CAPACITY).  out_dev: 58 doubles of device memory, written on `stream`.
+ * The first call on a device looks the array's address up (make it before any
+ * stream capture); calls that overlap on the GPU share the array and race. */
+GBF_API gbf_status gbf_reduce_noalloc(const gbf_reduce_inputs *in, const double T[16], float stddev,
+                                      double *out_dev, void *stream);
 /* Coarse-to-fine Gauss-Newton between the reference and current sets. Synchronises. */
 GBF_API gbf_status gbf_track(gbf_session *s, const double init[16], gbf_track_result *out, void *stream);
 /* Copy one pyramid image: kind 0 vmap, 1 nmap (float4), 2 intensity, 3 dI/dx,

@@ -55,6 +55,15 @@ class FrameStats(C.Structure):
                 ("render_blocks_valid", C.c_int32), ("status", C.c_uint32), ("track", TrackResult)]
 
 
+class ReduceInputs(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float),
+                ("ref_vmap", C.c_void_p), ("ref_nmap", C.c_void_p), ("ref_intensity", C.c_void_p),
+                ("cur_vmap", C.c_void_p), ("cur_nmap", C.c_void_p), ("cur_intensity", C.c_void_p),
+                ("cur_didx", C.c_void_p), ("cur_didy", C.c_void_p),
+                ("dist_thresh", C.c_float), ("angle_thresh", C.c_float)]
+
+
 class SynthParams(C.Structure):
     _fields_ = [("room", C.c_float * 3), ("n_spheres", C.c_int32), ("n_boxes", C.c_int32),
                 ("sphere_rmin", C.c_float), ("sphere_rmax", C.c_float), ("seed", C.c_uint64),
@@ -87,6 +96,7 @@ SIGNATURES = {
     "gbf_extract_mesh": (C.c_int, [_P, _I32, _P, _P, _U64, C.POINTER(C.c_uint64), _P]),
     "gbf_build_pyramid": (C.c_int, [_P, _I32, _P, _I64, _P, _I64, _P]),
     "gbf_reduce": (C.c_int, [_P, _I32, _D16, C.c_float, _D16, _P]),
+    "gbf_reduce_noalloc": (C.c_int, [C.POINTER(ReduceInputs), _D16, C.c_float, _P, _P]),
     "gbf_track": (C.c_int, [_P, _D16, C.POINTER(TrackResult), _P]),
     "gbf_get_image": (C.c_int, [_P, _I32, _I32, _I32, _P, _I64, _P]),
     "gbf_process_frame": (C.c_int, [_P, _P, _I64, _P, _I64, _P]),

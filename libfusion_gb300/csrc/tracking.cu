@@ -15,8 +15,12 @@
 // m_estimator.cu:477-479).  The order of every sum is fixed, so a session's
 // result does not depend on the other sessions in the batch.
 #include <float.h>
+#include <string.h>
+
+#include <mutex>
 
 #include "gbf_device.cuh"
+#include "gbf_internal.h"
 #include "gbf_kernels.h"
 
 namespace gbf {
@@ -466,3 +470,142 @@ void launch_frame_finish(const SessionView *d_sv, int nslots, cudaStream_t st) {
 }
 
 }  // namespace gbf
+
+// ============================================================================
+// Allocation-free ICP + photometric reduction.
+//
+// Some callers cannot allocate device memory at all: code running while a CUDA
+// graph is being captured (cudaMalloc is not capturable), real-time loops that
+// forbid allocation after start-up, and host frameworks that hand out every
+// byte of device memory through their own allocator.  For them this entry
+// point reduces one pyramid level of caller-owned images with no session and no
+// cudaMalloc / cudaFree: its per-CTA partial sums and its last-CTA ticket live
+// in the file-scope array below, which every GPU that loads the library keeps
+// until the process exits.
+namespace gbf {
+namespace {
+
+constexpr int kStaticReduceCtas = 2048;  // 2048 CTAs x 1024 pixels: up to 2,097,152 pixels per image
+constexpr int kStaticTicketSlot = kStaticReduceCtas * kPartialStride;
+
+// partial records of kStaticReduceCtas CTAs, then the ticket (as unsigned bits)
+static __device__ __align__(256) float g_reduce_scratch[kStaticTicketSlot + 64];
+
+__global__ void __launch_bounds__(kReduceThreads) reduce_static_kernel(SessionView sv, ReduceArgs a, float *scratch,
+                                                                       double *out) {
+    const int level = 0, rs = 0, cs = 1;
+    const int nctas = sv.red_ctas[0];
+    __shared__ M34 T;
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int i = 0; i < 12; ++i) T.m[i] = a.pose[i];
+    __syncthreads();
+    const int P = sv.lv[0].w * sv.lv[0].h;
+    float acc[kReduceWidth];
+#pragma unroll
+    for (int k = 0; k < kReduceWidth; ++k) acc[k] = 0.f;
+    const int stride = nctas * kReduceThreads;
+    for (int p = blockIdx.x * kReduceThreads + threadIdx.x; p < P; p += stride) {
+        float row[7];
+        if (icp_row(sv, level, rs, cs, T, p, row)) accumulate(acc, row);
+        if (rgb_row(sv, level, rs, cs, T, a.stddev, p, row)) accumulate(acc + 29, row);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < kReduceWidth; ++k) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
+    __shared__ float warp_sums[kReduceThreads / 32][kReduceWidth];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < kReduceWidth; ++k) warp_sums[wid][k] = acc[k];
+    __syncthreads();
+    if (threadIdx.x < kReduceWidth) {
+        float s = 0.f;
+#pragma unroll
+        for (int w = 0; w < kReduceThreads / 32; ++w) s += warp_sums[w][threadIdx.x];
+        scratch[(size_t)blockIdx.x * kPartialStride + threadIdx.x] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    __shared__ unsigned int ticket;
+    unsigned *tk = reinterpret_cast<unsigned *>(scratch + kStaticTicketSlot);
+    if (threadIdx.x == 0) ticket = atomicAdd(tk, 1u);
+    __syncthreads();
+    if (ticket != (unsigned)nctas - 1u) return;
+    __threadfence();
+    if (threadIdx.x < kReduceWidth) {
+        double s = 0.0;
+        for (int c = 0; c < nctas; ++c) s += (double)__ldcg(scratch + (size_t)c * kPartialStride + threadIdx.x);
+        out[threadIdx.x] = s;
+    }
+    if (threadIdx.x == 0) *tk = 0u;
+}
+
+// device address of g_reduce_scratch per device, looked up once with that device current
+std::mutex g_scratch_mu;
+float *g_scratch_ptr[64] = {};
+
+gbf_status static_scratch(float **ptr) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_error(e, "gbf_reduce_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= 64) return set_error(GBF_ERR_INVALID_ARG, "gbf_reduce_noalloc: device index >= 64");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_reduce_scratch);
+        if (e != cudaSuccess) return cuda_error(e, "gbf_reduce_noalloc: cudaGetSymbolAddress");
+        g_scratch_ptr[dev] = static_cast<float *>(p);
+    }
+    *ptr = g_scratch_ptr[dev];
+    return GBF_OK;
+}
+
+}  // namespace
+}  // namespace gbf
+
+extern "C" GBF_API gbf_status gbf_reduce_noalloc(const gbf_reduce_inputs *in, const double T[16], float stddev,
+                                                 double *out_dev, void *stream) {
+    using namespace gbf;
+    if (!in || !T || !out_dev || !in->ref_vmap || !in->ref_nmap || !in->ref_intensity || !in->cur_vmap ||
+        !in->cur_nmap || !in->cur_intensity || !in->cur_didx || !in->cur_didy)
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_reduce_noalloc: null pointer");
+    if (in->width < 8 || in->height < 8 || !(in->fx > 0) || !(in->fy > 0))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_reduce_noalloc: bad image size or focal length");
+    const long long pixels = (long long)in->width * in->height;
+    if (pixels > (long long)kStaticReduceCtas * kReduceThreads * kReducePixelsPerThread)
+        return set_error(GBF_ERR_CAPACITY, "gbf_reduce_noalloc: at most 2,097,152 pixels per image");
+    float *scratch = nullptr;
+    gbf_status st = static_scratch(&scratch);
+    if (st != GBF_OK) return st;
+    // a SessionView over the caller's level-0 images: set 0 = reference, set 1 = current
+    SessionView sv;
+    memset(&sv, 0, sizeof(sv));
+    sv.levels = 1;
+    LevelK &K = sv.lv[0];
+    K.w = in->width; K.h = in->height;
+    K.fx = in->fx; K.fy = in->fy; K.cx = in->cx; K.cy = in->cy;
+    K.invfx = 1.0f / in->fx; K.invfy = 1.0f / in->fy;
+    sv.red_ctas[0] = reduce_ctas((int)pixels);
+    sv.icp_dist = in->dist_thresh;
+    sv.icp_angle = in->angle_thresh;
+    sv.vmap[0][0] = (float4 *)in->ref_vmap;
+    sv.nmap[0][0] = (float4 *)in->ref_nmap;
+    sv.inten[0][0] = (float *)in->ref_intensity;
+    sv.vmap[1][0] = (float4 *)in->cur_vmap;
+    sv.nmap[1][0] = (float4 *)in->cur_nmap;
+    sv.inten[1][0] = (float *)in->cur_intensity;
+    sv.gx[0] = (float *)in->cur_didx;
+    sv.gy[0] = (float *)in->cur_didy;
+    ReduceArgs a{};
+    a.once = 1;
+    for (int i = 0; i < 12; ++i) a.pose[i] = (float)T[i];
+    a.stddev = stddev;
+    cudaStream_t s = (cudaStream_t)stream;
+    // the ticket must start at zero whatever an earlier, interrupted call left
+    cudaError_t e = cudaMemsetAsync(scratch + kStaticTicketSlot, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return cuda_error(e, "gbf_reduce_noalloc: clear ticket");
+    reduce_static_kernel<<<sv.red_ctas[0], kReduceThreads, 0, s>>>(sv, a, scratch, out_dev);
+    return check_cuda("gbf_reduce_noalloc");
+}
