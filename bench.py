@@ -153,10 +153,10 @@ def kernel_bytes(L, sessions, phase: str, K) -> float:
     total = 0.0
     for s in sessions:
         st = s.stats()
-        sv = 8 if s.cfg.voxel_layout == L.VOXEL_HALF else 10
+        sv = 8 if s.cfg.voxel_layout == L.VOXEL_HALF else 12
         if phase == "integrate":
-            # voxel read-modify-write of every visible block + depth/normal/colour gathers
-            total += 2.0 * sv * 512 * st.visible_blocks + P * (4 + 16 + 4)
+            # voxel read-modify-write of every visible block + per-pixel depth/weight and colour
+            total += 2.0 * sv * 512 * st.visible_blocks + P * (8 + 4)
         elif phase == "track":
             # fused ICP + photometric rows: ref vmap/nmap/intensity + cur vmap/nmap/I/dI per pixel-iteration
             its = sum(s.cfg.max_iterations[l] * (P >> (2 * l)) for l in range(s.cfg.num_levels))
@@ -438,7 +438,7 @@ def run_ours(args):
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"served: {S} concurrent 640x480 sessions per GPU, one frame each per tick",
                    "sessions_per_gpu": S, "voxel_m": list(VOXELS), "truncation": "clip(3*voxel, 2 cm, 3 cm)",
-                   "voxel_layout": "fp16 sdf + u16 weight + rgba8 (8 B/voxel)", "pool_blocks": 1 << 18,
+                   "voxel_layout": "fp16 sdf + fp16 weight + rgba8 (8 B/voxel)", "pool_blocks": 1 << 18,
                    "hash_slots": 1 << 19, "pyramid": "3 levels 10/5/3", "graph": use_graph,
                    "l2": "working set per tick (voxel pools, 64 x 640x480 pyramids) far above the 129 MB L2; no flush",
                    "inputs": "seeded synthetic RGB-D (sphere-traced SDF room, depth noise model) resident in HBM"},

@@ -68,7 +68,7 @@ enum {
 typedef enum gbf_voxel_layout {
     GBF_VOXEL_REF = 0,  /* int16 sdf (x32767, truncating) + f32 weight (<=255) + rgb8:
                            the reference Voxel semantics, include/data_struct/voxel.h:11-66 */
-    GBF_VOXEL_HALF = 1  /* fp16 sdf + u16 weight (w*256, <=255) + rgb8: 8 B per voxel */
+    GBF_VOXEL_HALF = 1  /* fp16 sdf + 16-bit weight (binary16, <=255) + rgb8: 8 B per voxel */
 } gbf_voxel_layout;
 
 typedef enum gbf_mesh_mode {

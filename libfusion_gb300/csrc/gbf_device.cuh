@@ -74,6 +74,24 @@ __device__ __forceinline__ void pose_copy(const double *a, double *b) {
     for (int i = 0; i < 12; ++i) b[i] = a[i];
 }
 
+// float forms of the mapping pose, computed once whenever map_pose changes
+__device__ __forceinline__ void update_map_floats(TrackState *ts) {
+    double inv[12];
+    pose_inverse(ts->map_pose, inv);
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+        ts->map_twc[i] = (float)ts->map_pose[i];
+        ts->map_tcw[i] = (float)inv[i];
+    }
+}
+
+__device__ __forceinline__ M34 load_m34(const float *m) {
+    M34 r;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) r.m[i] = m[i];
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // Vector3 helpers in the reference's order (include/math/vector_type.h)
 __device__ __forceinline__ float norm3(float x, float y, float z) {
@@ -90,13 +108,11 @@ __device__ __forceinline__ int floor_ref(float v) {
     return ((float)b > v) ? b - 1 : b;
 }
 
-// voxelPosToBlockPos (map_struct.cu:626-636)
-__device__ __forceinline__ int voxel_to_block(int v) { return (v < 0 ? v - 7 : v) / 8; }
-// voxelPosToLocalPos (map_struct.cu:643-655)
-__device__ __forceinline__ int voxel_to_local(int v) {
-    int r = v % 8;
-    return r < 0 ? r + 8 : r;
-}
+// voxelPosToBlockPos (map_struct.cu:626-636): (v < 0 ? v - 7 : v) / 8 with
+// truncating division is floor(v / 8), an arithmetic shift
+__device__ __forceinline__ int voxel_to_block(int v) { return v >> 3; }
+// voxelPosToLocalPos (map_struct.cu:643-655): v % 8, plus 8 when negative = v & 7
+__device__ __forceinline__ int voxel_to_local(int v) { return v & 7; }
 
 // computeHash (map_struct.cu:143-148) with defined 32-bit wraparound.
 __host__ __device__ __forceinline__ int compute_hash(int x, int y, int z, int n) {
@@ -117,11 +133,21 @@ __device__ __forceinline__ bool coord_ok(int x, int y, int z) {
            z < kCoordLimit;
 }
 
+// Home slot: computeHash modulo the slot count; for a power-of-two count the
+// non-negative remainder is the low bits.
+__device__ __forceinline__ int home_slot(const SessionView &sv, int x, int y, int z) {
+    if (sv.cap_mask >= 0) {
+        const unsigned ux = (unsigned)x * 73856093u, uy = (unsigned)y * 19349669u, uz = (unsigned)z * 83492791u;
+        return (int)((ux ^ uy ^ uz) & (unsigned)sv.cap_mask);
+    }
+    return compute_hash(x, y, z, sv.cap);
+}
+
 // Read-only lookup: pool block id or -1.
 __device__ __forceinline__ int find_block(const SessionView &sv, int bx, int by, int bz) {
     if (!coord_ok(bx, by, bz)) return -1;
     const unsigned long long key = pack_key(bx, by, bz);
-    int slot = compute_hash(bx, by, bz, sv.cap);
+    int slot = home_slot(sv, bx, by, bz);
     for (int p = 0; p < sv.max_probe; ++p) {
         const int4 e = __ldg(reinterpret_cast<const int4 *>(sv.table) + slot);
         const unsigned long long k = ((unsigned long long)(unsigned)e.y << 32) | (unsigned)e.x;
@@ -135,8 +161,8 @@ __device__ __forceinline__ int find_block(const SessionView &sv, int bx, int by,
 // ---------------------------------------------------------------------------
 // Voxel storage.  REF: int16 sdf packed as (short)(v*32767) (truncation),
 // unpacked as v/32767.f; float weight clamped to 255 (include/data_struct/
-// voxel.h:36-66).  HALF: fp16 sdf (round to nearest), weight as uint16 w*256
-// rounded to nearest, clamped to 255*256.
+// voxel.h:36-66).  HALF: fp16 sdf and fp16 weight (clamped to 255), both
+// rounded to nearest.
 struct Vox {
     float sdf;
     float w;
@@ -146,36 +172,61 @@ struct Vox {
 __device__ __forceinline__ float sdf_ref_unpack(short v) { return (float)v / 32767.f; }
 __device__ __forceinline__ short sdf_ref_pack(float v) { return (short)__float2int_rz(v * 32767.f); }
 __device__ __forceinline__ float weight_ref_store(float w) { return w > 255.f ? 255.f : w; }
+// HALF weight: the clamped float weight rounded to binary16 (11-bit significand,
+// range to 65504).  A linear 16-bit code over [0, 255] would quantise one
+// observation's weight (|sin n_z| / d^2, often below 0.1) by several percent.
 __device__ __forceinline__ unsigned short weight_half_pack(float w) {
-    float q = w * 256.f + 0.5f;
-    if (!(q < 65280.f)) q = 65280.f;
-    return (unsigned short)__float2uint_rz(q);
+    return __half_as_ushort(__float2half_rn(w > 255.f ? 255.f : w));
 }
-__device__ __forceinline__ float weight_half_unpack(unsigned short q) { return (float)q * (1.0f / 256.f); }
+__device__ __forceinline__ float weight_half_unpack(unsigned short q) { return __half2float(__ushort_as_half(q)); }
+
+// One load gives sdf and weight: HALF packs them in a 32-bit word, REF in 64 bits.
+template <int LAYOUT>
+__device__ __forceinline__ float unpack_sw(unsigned lo, unsigned hi, float &w) {
+    if (LAYOUT == GBF_VOXEL_REF) {
+        w = __uint_as_float(hi);
+        return sdf_ref_unpack((short)(lo & 0xffffu));
+    } else {
+        w = weight_half_unpack((unsigned short)(lo >> 16));
+        return __half2float(__ushort_as_half((unsigned short)(lo & 0xffffu)));
+    }
+}
 
 template <int LAYOUT>
 __device__ __forceinline__ Vox load_vox(const SessionView &sv, size_t i) {
     Vox v;
     if (LAYOUT == GBF_VOXEL_REF) {
-        v.sdf = sdf_ref_unpack(reinterpret_cast<const short *>(sv.vox_sdf)[i]);
-        v.w = reinterpret_cast<const float *>(sv.vox_w)[i];
+        const uint2 q = reinterpret_cast<const uint2 *>(sv.vox_sw)[i];
+        v.sdf = unpack_sw<LAYOUT>(q.x, q.y, v.w);
     } else {
-        v.sdf = __half2float(reinterpret_cast<const __half *>(sv.vox_sdf)[i]);
-        v.w = weight_half_unpack(reinterpret_cast<const unsigned short *>(sv.vox_w)[i]);
+        const unsigned q = reinterpret_cast<const unsigned *>(sv.vox_sw)[i];
+        v.sdf = unpack_sw<LAYOUT>(q, 0u, v.w);
     }
     v.rgb = sv.vox_rgb[i];
     return v;
 }
 
-// sdf + validity only (raycast / meshing).  Weight zero = unobserved.
+// sdf + weight through the read-only path (raycast / meshing).  Weight zero = unobserved.
 template <int LAYOUT>
 __device__ __forceinline__ float load_sdf(const SessionView &sv, size_t i, float &w) {
     if (LAYOUT == GBF_VOXEL_REF) {
-        w = __ldg(reinterpret_cast<const float *>(sv.vox_w) + i);
-        return sdf_ref_unpack(__ldg(reinterpret_cast<const short *>(sv.vox_sdf) + i));
+        const uint2 q = __ldg(reinterpret_cast<const uint2 *>(sv.vox_sw) + i);
+        return unpack_sw<LAYOUT>(q.x, q.y, w);
     } else {
-        w = weight_half_unpack(__ldg(reinterpret_cast<const unsigned short *>(sv.vox_w) + i));
-        return __half2float(__ldg(reinterpret_cast<const __half *>(sv.vox_sdf) + i));
+        const unsigned q = __ldg(reinterpret_cast<const unsigned *>(sv.vox_sw) + i);
+        return unpack_sw<LAYOUT>(q, 0u, w);
+    }
+}
+
+// store sdf + weight with the layout's quantisation (voxel.h:36-66 for REF)
+template <int LAYOUT>
+__device__ __forceinline__ void store_sw(const SessionView &sv, size_t i, float sdf, float w) {
+    if (LAYOUT == GBF_VOXEL_REF) {
+        reinterpret_cast<uint2 *>(sv.vox_sw)[i] =
+            make_uint2((unsigned)(unsigned short)sdf_ref_pack(sdf), __float_as_uint(weight_ref_store(w)));
+    } else {
+        reinterpret_cast<unsigned *>(sv.vox_sw)[i] =
+            (unsigned)__half_as_ushort(__float2half_rn(sdf)) | ((unsigned)weight_half_pack(w) << 16);
     }
 }
 
@@ -200,7 +251,7 @@ __device__ __forceinline__ int warp_append(int *counter, bool pred) {
 
 // Insert (or find) one block in the session table; stamps it with `frame`.
 __device__ __forceinline__ int insert_block(const SessionView &sv, unsigned long long key, int bx, int by, int bz, int frame) {
-    int slot = compute_hash(bx, by, bz, sv.cap);
+    int slot = home_slot(sv, bx, by, bz);
     for (int p = 0; p < sv.max_probe; ++p) {
         HashSlot *e = sv.table + slot;
         unsigned long long k = __ldcg(&e->key);

@@ -23,8 +23,8 @@ gbf_status check_cuda(const char *where);
 // Byte layout of one session's device arena.
 struct ArenaLayout {
     size_t total;
-    size_t table, bcoord, bstamp, bfresh, vis, mesh_off, vox_sdf, vox_w, vox_rgb, ctr, ts;
-    size_t in_depth, in_rgb, depth_raw, rgb4, nmap_ext, zr_min, zr_max, partials;
+    size_t table, bcoord, bstamp, bfresh, vis, mesh_off, vox_sw, vox_rgb, ctr, ts;
+    size_t in_depth, in_rgb, depth_raw, rgb4, nmap_ext, fuse_px, zr_min, zr_max, partials;
     size_t depth[kMaxLevels], inten[2][kMaxLevels], gx[kMaxLevels], gy[kMaxLevels];
     size_t vmap[2][kMaxLevels], nmap[2][kMaxLevels];
 };

@@ -57,6 +57,8 @@ enum Counter {
 struct TrackState {
     double pose[12];       // T_wc of the newest frame (3x4 row-major)
     double map_pose[12];   // pose used by fuse / raycast
+    float map_twc[12];     // map_pose and its inverse rounded to float (the reference's
+    float map_tcw[12];     // pose.cast<float>() / pose.inverse().cast<float>())
     double est[12];        // Revertable<SE3d> current (icp_tracker.cpp:25)
     double est_prev[12];   // Revertable<SE3d> previous
     double init[12];       // initial estimate of the current tracking run
@@ -79,6 +81,7 @@ struct SessionView {
     int active;
     int layout;            // gbf_voxel_layout
     int cap, pool, max_probe;
+    int cap_mask;          // cap - 1 when cap is a power of two, else -1
     float voxel, inv_voxel, tau, inv_tau, step_scale;
     float zmin_u, zmax_u, zmin_r, zmax_r, block_metric;
     float w_icp, w_rgb, icp_dist, icp_angle;
@@ -93,8 +96,8 @@ struct SessionView {
     int4 *bcoord;          // per pool block: x, y, z, slot
     int *bstamp;           // fuse counter of the last touch
     unsigned char *bfresh; // 1 = voxels not yet initialised
-    void *vox_sdf;         // int16 (REF) or half (HALF), 512 per block
-    void *vox_w;           // float (REF) or uint16 (HALF)
+    void *vox_sw;          // sdf + weight word per voxel, 512 per block: HALF uint32
+                           // (fp16 sdf | fp16 weight << 16), REF uint2 (int16 sdf, f32 weight)
     uchar4 *vox_rgb;
     int *vis;              // visible block ids
     int *ctr;              // Counter array
@@ -105,6 +108,7 @@ struct SessionView {
     float *depth_raw;      // level-0 metres, unfiltered (fused)
     uchar4 *rgb4;          // level-0 colour (fused)
     float4 *nmap_ext;      // imported normal map (gbf_fuse)
+    float2 *fuse_px;       // per pixel of the fused frame: (depth or NaN if rejected, weight)
     float *depth[kMaxLevels];
     float *inten[2][kMaxLevels];
     float *gx[kMaxLevels];

@@ -154,6 +154,16 @@ __device__ __forceinline__ float4 normal_from(float4 v00, float4 v01, float4 v10
     return make_float4(n.x / l, n.y / l, n.z / l, 1.f);
 }
 
+// Integration test and weight of the frame's pixel for the normal-weighted
+// update (update_map_weighted_kernel, depth_fusion.cu:390-405): raw depth,
+// level-0 normal of the filtered depth; rejected pixels carry NaN depth.
+__device__ __forceinline__ void fuse_weight(const SessionView &sv, int i, float4 n) {
+    const float dist = sv.depth_raw[i];
+    const bool ok = !(isnan(dist) || isnan(n.x) || dist > sv.zmax_u || dist < sv.zmin_u);
+    const float w = fabsf(sinf(n.z)) / (dist * dist);
+    sv.fuse_px[i] = make_float2(ok ? dist : __int_as_float(0x7fffffff), w);
+}
+
 __global__ void level_maps_kernel(const SessionView *svs, int set_sel, int tiles_per_level0) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
@@ -182,12 +192,15 @@ __global__ void level_maps_kernel(const SessionView *svs, int set_sel, int tiles
         const float4 v01 = back_project(D, K.w, x + 1, y, K);
         const float4 v10 = back_project(D, K.w, x, y10, K);
         const float4 v11 = back_project(D, K.w, x, y + 1, K);
-        sv.nmap[set][level][i] = normal_from(v00, v01, v10, v11);
+        const float4 n = normal_from(v00, v01, v10, v11);
+        sv.nmap[set][level][i] = n;
+        if (level == 0 && set_sel == 0) fuse_weight(sv, i, n);
     } else {
         // the reference leaves the last row / column unwritten; write invalid
         sv.gx[level][i] = 0.f;
         sv.gy[level][i] = 0.f;
         sv.nmap[set][level][i] = make_float4(nanf_, nanf_, nanf_, nanf_);
+        if (level == 0 && set_sel == 0) fuse_weight(sv, i, make_float4(nanf_, nanf_, nanf_, nanf_));
     }
     sv.vmap[set][level][i] = back_project(D, K.w, x, y, K);
 }

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kAllocTile *kAllocTile) alloc_kernel(const Ses
     __shared__ unsigned long long set[kSetSize];
     __shared__ M34 T;
     for (int i = threadIdx.x; i < kSetSize; i += blockDim.x) set[i] = kEmptyKey;
-    if (threadIdx.x == 0) T = pose_to_float(sv.ts->map_pose);
+    if (threadIdx.x == 0) T = load_m34(sv.ts->map_twc);
     __syncthreads();
     const int frame = sv.ctr[C_FRAME];
 
@@ -152,6 +152,30 @@ __global__ void __launch_bounds__(kAllocTile *kAllocTile) alloc_kernel(const Ses
     }
 }
 
+// Per-pixel part of the integration test and weight (update_map_with_colour_kernel,
+// depth_fusion.cu:317-331, mode 0; update_map_weighted_kernel, :390-405, mode 2):
+// every voxel projecting to a pixel shares them, so they are computed once per
+// pixel.  Mode 1 (System frames) gets the same values from level_maps_kernel.
+__global__ void fuse_prep_kernel(const SessionView *svs, int mode) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active) return;
+    const int n = sv.lv[0].w * sv.lv[0].h;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float dist = sv.depth_raw[i];
+    bool ok;
+    float w;
+    if (mode == 0) {
+        ok = !(isnan(dist) || (double)dist < 1e-2 || dist > sv.zmax_u || dist < sv.zmin_u);
+        w = 1.0f / (dist * dist);
+    } else {
+        const float4 nc = sv.nmap_ext[i];
+        ok = !(isnan(dist) || isnan(nc.x) || dist > sv.zmax_u || dist < sv.zmin_u);
+        w = fabsf(sinf(nc.z)) / (dist * dist);
+    }
+    sv.fuse_px[i] = make_float2(ok ? dist : __int_as_float(0x7fffffff), w);
+}
+
 // is_vertex_visible / is_block_visible (depth_fusion.cu:15-47)
 __device__ __forceinline__ bool block_in_frustum(const SessionView &sv, const M34 &Tcw, int bx, int by, int bz) {
     const LevelK &K = sv.lv[0];
@@ -172,11 +196,7 @@ __global__ void visible_kernel(const SessionView *svs) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     __shared__ M34 Tcw;
-    if (threadIdx.x == 0) {
-        double inv[12];
-        pose_inverse(sv.ts->map_pose, inv);
-        Tcw = pose_to_float(inv);
-    }
+    if (threadIdx.x == 0) Tcw = load_m34(sv.ts->map_tcw);
     __syncthreads();
     const int frame = sv.ctr[C_FRAME];
     const int n = min(sv.ctr[C_NUSED], sv.pool);
@@ -201,16 +221,11 @@ __global__ void __launch_bounds__(256) integrate_kernel(const SessionView *svs, 
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || sv.layout != LAYOUT) return;
     __shared__ M34 Tcw;
-    if (threadIdx.x == 0) {
-        double inv[12];
-        pose_inverse(sv.ts->map_pose, inv);
-        Tcw = pose_to_float(inv);
-    }
+    if (threadIdx.x == 0) Tcw = load_m34(sv.ts->map_tcw);
     __syncthreads();
     const LevelK &K = sv.lv[0];
     const int W = K.w, H = K.h;
     const int nvis = sv.ctr[C_NVIS];
-    const float4 *nmap = (mode == 1) ? sv.nmap[sv.ts->idx][0] : sv.nmap_ext;
     const float voxel = sv.voxel, tau = sv.tau, inv_tau = sv.inv_tau;
 
     for (int b = blockIdx.x; b < nvis; b += gridDim.x) {
@@ -228,16 +243,13 @@ __global__ void __launch_bounds__(256) integrate_kernel(const SessionView *svs, 
             const int u = __float2int_rd(((K.fx * p.x) / p.z + K.cx) + 0.5f);
             const int v = __float2int_rd(((K.fy * p.y) / p.z + K.cy) + 0.5f);
             bool upd = !(u < 0 || v < 0 || u > W - 1 || v > H - 1);
-            float dist = 0.f, nz = 0.f, sdf = 0.f;
+            float dist = 0.f, weight = 0.f, sdf = 0.f;
             if (upd) {
-                dist = sv.depth_raw[(size_t)v * W + u];
-                if (mode == 0) {
-                    upd = !(isnan(dist) || (double)dist < 1e-2 || dist > sv.zmax_u || dist < sv.zmin_u);
-                } else {
-                    const float4 n = nmap[(size_t)v * W + u];
-                    nz = n.z;
-                    upd = !(isnan(dist) || isnan(n.x) || dist > sv.zmax_u || dist < sv.zmin_u);
-                }
+                // depth and weight of the pixel, rejected pixels as NaN (fuse_px)
+                const float2 fp = sv.fuse_px[(size_t)v * W + u];
+                dist = fp.x;
+                weight = fp.y;
+                upd = !isnan(dist);
             }
             if (upd) {
                 sdf = dist - p.z;
@@ -245,13 +257,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const SessionView *svs, 
             }
             if (!upd) {
                 if (fresh) {
-                    if (LAYOUT == GBF_VOXEL_REF) {
-                        reinterpret_cast<short *>(sv.vox_sdf)[vi] = 0;
-                        reinterpret_cast<float *>(sv.vox_w)[vi] = 0.f;
-                    } else {
-                        reinterpret_cast<__half *>(sv.vox_sdf)[vi] = __float2half_rn(0.f);
-                        reinterpret_cast<unsigned short *>(sv.vox_w)[vi] = 0;
-                    }
+                    store_sw<LAYOUT>(sv, vi, 0.f, 0.f);
                     sv.vox_rgb[vi] = make_uchar4(0, 0, 0, 0);
                 }
                 continue;
@@ -263,7 +269,6 @@ __global__ void __launch_bounds__(256) integrate_kernel(const SessionView *svs, 
             } else {
                 old = load_vox<LAYOUT>(sv, vi);
             }
-            const float weight = (mode == 0) ? 1.0f / (dist * dist) : fabsf(sinf(nz)) / (dist * dist);
             const uchar4 cn = sv.rgb4[(size_t)v * W + u];
             float nsdf, nw;
             uchar4 nrgb;
@@ -278,13 +283,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const SessionView *svs, 
                 nrgb.z = (unsigned char)__float2int_rz(((float)old.rgb.z * old.w + (float)cn.z * weight) / den);
                 nrgb.w = 0;
             }
-            if (LAYOUT == GBF_VOXEL_REF) {
-                reinterpret_cast<short *>(sv.vox_sdf)[vi] = sdf_ref_pack(nsdf);
-                reinterpret_cast<float *>(sv.vox_w)[vi] = weight_ref_store(nw);
-            } else {
-                reinterpret_cast<__half *>(sv.vox_sdf)[vi] = __float2half_rn(nsdf);
-                reinterpret_cast<unsigned short *>(sv.vox_w)[vi] = weight_half_pack(nw);
-            }
+            store_sw<LAYOUT>(sv, vi, nsdf, nw);
             sv.vox_rgb[vi] = nrgb;
         }
         if (fresh && threadIdx.x == 0) sv.bfresh[id] = 0;
@@ -308,6 +307,7 @@ void launch_alloc_visible(const SessionView *d_sv, int nslots, const Extent &ex,
 
 void launch_integrate(const SessionView *d_sv, int nslots, const Extent &ex, int mode, const int *layouts,
                       cudaStream_t st) {
+    if (mode != 1) fuse_prep_kernel<<<dim3((ex.w * ex.h + 255) / 256, nslots), 256, 0, st>>>(d_sv, mode);
     // one CTA per visible block, grid-stride; 8 resident CTAs of 256 threads per SM
     const int gi = 152 * 8;
     if (layouts[GBF_VOXEL_REF]) integrate_kernel<GBF_VOXEL_REF><<<dim3(gi, nslots), 256, 0, st>>>(d_sv, mode);

@@ -37,11 +37,7 @@ __global__ void zrange_kernel(const SessionView *svs) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     __shared__ M34 Tcw;
-    if (threadIdx.x == 0) {
-        double inv[12];
-        pose_inverse(sv.ts->map_pose, inv);
-        Tcw = pose_to_float(inv);
-    }
+    if (threadIdx.x == 0) Tcw = load_m34(sv.ts->map_tcw);
     __syncthreads();
     const int nvis = sv.ctr[C_NVIS];
     const LevelK &K = sv.lv[0];
@@ -82,23 +78,30 @@ __global__ void zrange_kernel(const SessionView *svs) {
     }
 }
 
+// Last block lookup of a ray: consecutive samples usually stay in one block.
 struct BlockCache {
     int bx, by, bz, id;
+    __device__ __forceinline__ void init() {
+        bx = by = bz = 0x7fffffff;
+        id = -1;
+    }
+    __device__ __forceinline__ int get(const SessionView &sv, int x, int y, int z) {
+        if (x != bx || y != by || z != bz) {
+            bx = x; by = y; bz = z;
+            id = find_block(sv, x, y, z);
+        }
+        return id;
+    }
 };
 
-// read_sdf (ray_tracing.cu:291-305): nearest voxel, NaN when unallocated or unobserved
+// One voxel by integer position: sdf, or NaN when unallocated or unobserved.
 template <int LAYOUT>
-__device__ __forceinline__ float read_sdf(const SessionView &sv, BlockCache &bc, float px, float py, float pz,
+__device__ __forceinline__ float read_vox(const SessionView &sv, BlockCache &bc, int vx, int vy, int vz,
                                           bool &valid) {
-    const int vx = floor_ref(px), vy = floor_ref(py), vz = floor_ref(pz);
-    const int bx = voxel_to_block(vx), by = voxel_to_block(vy), bz = voxel_to_block(vz);
-    if (bx != bc.bx || by != bc.by || bz != bc.bz) {
-        bc.bx = bx; bc.by = by; bc.bz = bz;
-        bc.id = find_block(sv, bx, by, bz);
-    }
-    if (bc.id >= 0) {
-        const size_t i = (size_t)bc.id * kBlockVoxels + (voxel_to_local(vz) * 64 + voxel_to_local(vy) * 8 +
-                                                          voxel_to_local(vx));
+    const int id = bc.get(sv, voxel_to_block(vx), voxel_to_block(vy), voxel_to_block(vz));
+    if (id >= 0) {
+        const size_t i = (size_t)id * kBlockVoxels + (voxel_to_local(vz) * 64 + voxel_to_local(vy) * 8 +
+                                                      voxel_to_local(vx));
         float w;
         const float s = load_sdf<LAYOUT>(sv, i, w);
         if (w != 0.f) {
@@ -110,31 +113,50 @@ __device__ __forceinline__ float read_sdf(const SessionView &sv, BlockCache &bc,
     return __int_as_float(0x7fffffff);
 }
 
-// read_sdf_interped (ray_tracing.cu:307-339)
+// read_sdf (ray_tracing.cu:291-305): nearest voxel ToVector3i(pt)
 template <int LAYOUT>
+__device__ __forceinline__ float read_sdf(const SessionView &sv, BlockCache &bc, float px, float py, float pz,
+                                          bool &valid) {
+    return read_vox<LAYOUT>(sv, bc, floor_ref(px), floor_ref(py), floor_ref(pz), valid);
+}
+
+// read_sdf_interped (ray_tracing.cu:307-339).  The reference reads the eight
+// corners at pt + (0|1, 0|1, 0|1) and floors each sum; the six per-axis floors
+// floor(p), floor(p + 1) are computed once (floor(p + 1) is not always
+// floor(p) + 1 in float).  s000 / v000: the corner at floor(pt) when the caller
+// has already read it.
+template <int LAYOUT, bool HAVE000>
 __device__ __forceinline__ float read_sdf_interped(const SessionView &sv, BlockCache &bc, float px, float py,
-                                                   float pz, bool &valid) {
+                                                   float pz, bool &valid, float s000 = 0.f, bool v000 = false) {
     const float fx = px - floorf(px), fy = py - floorf(py), fz = pz - floorf(pz);
+    const int x0 = floor_ref(px + 0.0f), x1 = floor_ref(px + 1.0f);
+    const int y0 = floor_ref(py + 0.0f), y1 = floor_ref(py + 1.0f);
+    const int z0 = floor_ref(pz + 0.0f), z1 = floor_ref(pz + 1.0f);
     bool vpt, v;
     float s0, s1, r0, r1, r2, r3;
-    s0 = read_sdf<LAYOUT>(sv, bc, px, py, pz, vpt);
-    s1 = read_sdf<LAYOUT>(sv, bc, px + 1.0f, py + 0.0f, pz + 0.0f, v);
+    if (HAVE000) {
+        s0 = s000;
+        vpt = v000;
+    } else {
+        s0 = read_vox<LAYOUT>(sv, bc, x0, y0, z0, vpt);
+    }
+    s1 = read_vox<LAYOUT>(sv, bc, x1, y0, z0, v);
     vpt &= v;
     r0 = (1.0f - fx) * s0 + fx * s1;
-    s0 = read_sdf<LAYOUT>(sv, bc, px + 0.0f, py + 1.0f, pz + 0.0f, v);
+    s0 = read_vox<LAYOUT>(sv, bc, x0, y1, z0, v);
     vpt &= v;
-    s1 = read_sdf<LAYOUT>(sv, bc, px + 1.0f, py + 1.0f, pz + 0.0f, v);
+    s1 = read_vox<LAYOUT>(sv, bc, x1, y1, z0, v);
     vpt &= v;
     r1 = (1.0f - fx) * s0 + fx * s1;
     r2 = (1.0f - fy) * r0 + fy * r1;
-    s0 = read_sdf<LAYOUT>(sv, bc, px + 0.0f, py + 0.0f, pz + 1.0f, v);
+    s0 = read_vox<LAYOUT>(sv, bc, x0, y0, z1, v);
     vpt &= v;
-    s1 = read_sdf<LAYOUT>(sv, bc, px + 1.0f, py + 0.0f, pz + 1.0f, v);
+    s1 = read_vox<LAYOUT>(sv, bc, x1, y0, z1, v);
     vpt &= v;
     r0 = (1.0f - fx) * s0 + fx * s1;
-    s0 = read_sdf<LAYOUT>(sv, bc, px + 0.0f, py + 1.0f, pz + 1.0f, v);
+    s0 = read_vox<LAYOUT>(sv, bc, x0, y1, z1, v);
     vpt &= v;
-    s1 = read_sdf<LAYOUT>(sv, bc, px + 1.0f, py + 1.0f, pz + 1.0f, v);
+    s1 = read_vox<LAYOUT>(sv, bc, x1, y1, z1, v);
     vpt &= v;
     r1 = (1.0f - fx) * s0 + fx * s1;
     r3 = (1.0f - fy) * r0 + fy * r1;
@@ -158,10 +180,8 @@ __global__ void __launch_bounds__(kRayTileW *kRayTileH) raycast_kernel(const Ses
     const int y = (blockIdx.x / tiles_x) * kRayTileH + (threadIdx.x / kRayTileW);
     __shared__ M34 Twc, Tcw;
     if (threadIdx.x == 0) {
-        double inv[12];
-        pose_inverse(sv.ts->map_pose, inv);
-        Tcw = pose_to_float(inv);
-        Twc = pose_to_float(sv.ts->map_pose);
+        Tcw = load_m34(sv.ts->map_tcw);
+        Twc = load_m34(sv.ts->map_twc);
     }
     __syncthreads();
     if (x >= K.w || y >= K.h) return;
@@ -192,13 +212,14 @@ __global__ void __launch_bounds__(kRayTileW *kRayTileH) raycast_kernel(const Ses
     dir = make_float3(dir.x / dn, dir.y / dn, dir.z / dn);
     float3 r = bs;
 
-    BlockCache bc{0x7fffffff, 0x7fffffff, 0x7fffffff, -1};
+    BlockCache bc;
+    bc.init();
     float sdf = 1.0f, last_sdf, step;
     bool valid = false;
     for (int it = 0; dist_s < dist_e && it < kMaxMarch; ++it) {
         last_sdf = sdf;
         sdf = read_sdf<LAYOUT>(sv, bc, r.x, r.y, r.z, valid);
-        if (sdf <= 0.5f && sdf >= -0.5f) sdf = read_sdf_interped<LAYOUT>(sv, bc, r.x, r.y, r.z, valid);
+        if (sdf <= 0.5f && sdf >= -0.5f) sdf = read_sdf_interped<LAYOUT, true>(sv, bc, r.x, r.y, r.z, valid, sdf, valid);
         if (sdf <= 0.0f) break;
         if (sdf >= 0.f && last_sdf < 0.f) return;
         step = valid ? fmaxf(sdf * sv.step_scale, 1.0f) : 2.0f;
@@ -209,7 +230,7 @@ __global__ void __launch_bounds__(kRayTileW *kRayTileH) raycast_kernel(const Ses
     if (sdf <= 0.0f) {
         step = sdf * sv.step_scale;
         r = make_float3(r.x + dir.x * step, r.y + dir.y * step, r.z + dir.z * step);
-        sdf = read_sdf_interped<LAYOUT>(sv, bc, r.x, r.y, r.z, valid);
+        sdf = read_sdf_interped<LAYOUT, false>(sv, bc, r.x, r.y, r.z, valid);
         step = sdf * sv.step_scale;
         r = make_float3(r.x + dir.x * step, r.y + dir.y * step, r.z + dir.z * step);
         found = valid;

@@ -89,8 +89,7 @@ ArenaLayout plan_arena(const gbf_config &c, const gbf_intrinsics &K) {
     a.bfresh = take(pool);
     a.vis = take(pool * sizeof(int));
     a.mesh_off = take((pool + 1) * sizeof(int));
-    a.vox_sdf = take(nv * 2);
-    a.vox_w = take(nv * (c.voxel_layout == GBF_VOXEL_REF ? 4 : 2));
+    a.vox_sw = take(nv * (c.voxel_layout == GBF_VOXEL_REF ? 8 : 4));
     a.vox_rgb = take(nv * 4);
     a.ctr = take(C_COUNT * sizeof(int));
     a.ts = take(sizeof(TrackState));
@@ -100,6 +99,7 @@ ArenaLayout plan_arena(const gbf_config &c, const gbf_intrinsics &K) {
     a.depth_raw = take(P * 4);
     a.rgb4 = take(P * 4);
     a.nmap_ext = take(P * 16);
+    a.fuse_px = take(P * 8);
     size_t w = K.width, h = K.height;
     for (int l = 0; l < c.num_levels; ++l) {
         const size_t p = w * h;
@@ -174,13 +174,7 @@ __global__ void import_kernel(const SessionView *svs, int count, const int *coor
         if (id >= 0) {
             for (int i = threadIdx.x; i < kBlockVoxels; i += blockDim.x) {
                 const size_t o = (size_t)b * kBlockVoxels + i, vi = (size_t)id * kBlockVoxels + i;
-                if (LAYOUT == GBF_VOXEL_REF) {
-                    reinterpret_cast<short *>(sv.vox_sdf)[vi] = sdf_ref_pack(sdf[o]);
-                    reinterpret_cast<float *>(sv.vox_w)[vi] = weight_ref_store(w[o]);
-                } else {
-                    reinterpret_cast<__half *>(sv.vox_sdf)[vi] = __float2half_rn(sdf[o]);
-                    reinterpret_cast<unsigned short *>(sv.vox_w)[vi] = weight_half_pack(w[o]);
-                }
+                store_sw<LAYOUT>(sv, vi, sdf[o], w[o]);
                 sv.vox_rgb[vi] = make_uchar4(rgb[o * 3], rgb[o * 3 + 1], rgb[o * 3 + 2], 0);
             }
             if (threadIdx.x == 0) sv.bfresh[id] = 0;
@@ -215,6 +209,7 @@ TrackState initial_track_state() {
         t.pose[i] = t.map_pose[i] = t.est[i] = t.est_prev[i] = t.init[i] = t.update[i] = v;
     }
     t.icp_error = t.rgb_error = FLT_MAX;
+    for (int i = 0; i < 12; ++i) t.map_twc[i] = t.map_tcw[i] = (float)t.map_pose[i];
     return t;
 }
 
@@ -241,11 +236,16 @@ void to44(const double o[12], double T[16]) {
     T[15] = 1.0;
 }
 
+__global__ void map_pose_kernel(TrackState *ts) { update_map_floats(ts); }
+
 gbf_status set_map_pose(gbf_session *s, const double T[16], cudaStream_t st) {
     double p[12];
     to34(T, p);
     // pageable source: the copy is staged before the call returns
-    return cuda_error(cudaMemcpyAsync(s->view.ts->map_pose, p, sizeof(p), cudaMemcpyHostToDevice, st), "set pose");
+    cudaError_t e = cudaMemcpyAsync(s->view.ts->map_pose, p, sizeof(p), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_error(e, "set pose");
+    map_pose_kernel<<<1, 1, 0, st>>>(s->view.ts);
+    return check_cuda("set pose");
 }
 
 // One frame for `nslots` slots.  With `ev` (kPhases + 1 events) the phase
@@ -369,6 +369,7 @@ GBF_API gbf_status gbf_session_create(const gbf_config *cfg, const gbf_intrinsic
     v.active = 1;
     v.layout = cfg->voxel_layout;
     v.cap = cfg->num_buckets;
+    v.cap_mask = (cfg->num_buckets & (cfg->num_buckets - 1)) == 0 ? cfg->num_buckets - 1 : -1;
     v.pool = cfg->num_blocks;
     v.max_probe = cfg->max_probe;
     v.voxel = cfg->voxel_size;
@@ -394,8 +395,7 @@ GBF_API gbf_status gbf_session_create(const gbf_config *cfg, const gbf_intrinsic
     v.bfresh = reinterpret_cast<unsigned char *>(base + a.bfresh);
     v.vis = reinterpret_cast<int *>(base + a.vis);
     v.mesh_off = reinterpret_cast<int *>(base + a.mesh_off);
-    v.vox_sdf = base + a.vox_sdf;
-    v.vox_w = base + a.vox_w;
+    v.vox_sw = base + a.vox_sw;
     v.vox_rgb = reinterpret_cast<uchar4 *>(base + a.vox_rgb);
     v.ctr = reinterpret_cast<int *>(base + a.ctr);
     v.ts = reinterpret_cast<TrackState *>(base + a.ts);
@@ -404,6 +404,7 @@ GBF_API gbf_status gbf_session_create(const gbf_config *cfg, const gbf_intrinsic
     v.depth_raw = reinterpret_cast<float *>(base + a.depth_raw);
     v.rgb4 = reinterpret_cast<uchar4 *>(base + a.rgb4);
     v.nmap_ext = reinterpret_cast<float4 *>(base + a.nmap_ext);
+    v.fuse_px = reinterpret_cast<float2 *>(base + a.fuse_px);
     for (int l = 0; l < cfg->num_levels; ++l) {
         v.depth[l] = reinterpret_cast<float *>(base + a.depth[l]);
         v.gx[l] = reinterpret_cast<float *>(base + a.gx[l]);
@@ -488,6 +489,7 @@ GBF_API gbf_status gbf_set_pose(gbf_session *s, const double T[16], void *stream
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = cudaMemcpyAsync(s->view.ts->pose, p, sizeof(p), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->view.ts->map_pose, p, sizeof(p), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) map_pose_kernel<<<1, 1, 0, st>>>(s->view.ts);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     return cuda_error(e, "gbf_set_pose");
 }

@@ -147,19 +147,21 @@ __device__ __forceinline__ float interp2(const float *img, int w, float x, float
 }
 
 // ICPReduction::searchPoint + getRow (pose_estimator.cu:168-222)
-__device__ __forceinline__ bool icp_row(const SessionView &sv, int level, int rs, int cs, const M34 &T, int p,
-                                        float row[7]) {
+__device__ __forceinline__ bool icp_row(const SessionView &sv, int level, int cs, const M34 &T, const float4 vl,
+                                        const float4 nl4, float row[7]) {
     const LevelK &K = sv.lv[level];
-    const float4 vl = sv.vmap[rs][level][p];
     if (isnan(vl.x)) return false;
     const float3 vg = T.apply(vl.x, vl.y, vl.z);
-    const float invz = (float)(1.0 / (double)vg.z);
+    // float invz = 1.0 / vlast_g.z in the reference: a double division rounded to
+    // float.  For a float z that equals the correctly rounded float reciprocal
+    // (1/z lies at least 2^-49 relative from any 25-bit rounding midpoint, so
+    // the double rounding cannot change it), computed without FP64 hardware.
+    const float invz = __frcp_rn(vg.z);
     const int u = __float2int_rd(((vg.x * invz) * K.fx + K.cx) + 0.5f);
     const int v = __float2int_rd(((vg.y * invz) * K.fy + K.cy) + 0.5f);
     if (u < 0 || v < 0 || u >= K.w || v >= K.h) return false;
     const int q = v * K.w + u;
     const float4 vc4 = sv.vmap[cs][level][q];
-    const float4 nl4 = sv.nmap[rs][level][p];
     const float3 ng = T.rotate(nl4.x, nl4.y, nl4.z);
     const float4 nc4 = sv.nmap[cs][level][q];
     const float dist = norm3(vg.x - vc4.x, vg.y - vc4.y, vg.z - vc4.z);
@@ -173,13 +175,27 @@ __device__ __forceinline__ bool icp_row(const SessionView &sv, int level, int rs
     return true;
 }
 
+// Photometric constants of one reduction, evaluated once per CTA in the
+// reference's double precision (m_estimator.cu:366-373).
+struct PhotoConst {
+    float stddev, huber;
+    bool normalise, robust;
+};
+__device__ __forceinline__ PhotoConst photo_const(float stddev) {
+    PhotoConst c;
+    c.stddev = stddev;
+    c.normalise = (double)stddev > 10e-5;
+    c.robust = (double)stddev > 10e-6;
+    c.huber = (float)(1.345 * (double)stddev);
+    return c;
+}
+
 // RgbReduction2::find_corresp + compute_jacobian (m_estimator.cu:315-391)
-__device__ __forceinline__ bool rgb_row(const SessionView &sv, int level, int rs, int cs, const M34 &T, float stddev,
-                                        int p, float row[7]) {
+__device__ __forceinline__ bool rgb_row(const SessionView &sv, int level, int cs, const M34 &T,
+                                        const PhotoConst &pc, const float4 pt, const float il, float row[7]) {
+    const float stddev = pc.stddev;
     const LevelK &K = sv.lv[level];
-    const float4 pt = sv.vmap[rs][level][p];
     if (pt.w < 0 || isnan(pt.x)) return false;
-    const float il = sv.inten[rs][level][p];
     if (!isfinite(il)) return false;
     const float3 q = T.apply(pt.x, pt.y, pt.z);
     const float u0 = (q.x / q.z) * K.fx + K.cx;
@@ -189,14 +205,14 @@ __device__ __forceinline__ bool rgb_row(const SessionView &sv, int level, int rs
     const float dx = interp2(sv.gx[level], K.w, u0, v0);
     const float dy = interp2(sv.gy[level], K.w, u0, v0);
     if (!((dx > 2 || dy > 2) && isfinite(ic) && isfinite(dx) && isfinite(dy))) return false;
-    const float zi = (float)(1.0 / (double)q.z);
+    const float zi = __frcp_rn(q.z);  // float z_inv = 1.0 / z (same argument as icp_row)
     const float lx = (dx * K.fx) * zi, ly = (dy * K.fy) * zi;
     const float lz = (-(lx * q.x + ly * q.y)) * zi;
     float res = ic - il;
-    if ((double)stddev > 10e-5) res /= stddev;
-    const float huber = (float)(1.345 * (double)stddev);
+    if (pc.normalise) res /= stddev;
+    const float huber = pc.huber;
     float w = 1.f;
-    if (fabsf(res) > huber && (double)stddev > 10e-6) w = sqrtf(huber / fabsf(res));
+    if (fabsf(res) > huber && pc.robust) w = sqrtf(huber / fabsf(res));
     const float3 pl = cross3(q, make_float3(lx, ly, lz));
     row[0] = lx * w; row[1] = ly * w; row[2] = lz * w;
     row[3] = pl.x * w; row[4] = pl.y * w; row[5] = pl.z * w;
@@ -213,6 +229,92 @@ __device__ __forceinline__ void accumulate(float *acc, const float row[7]) {
     acc[28] += 1.0f;
 }
 
+constexpr int kCtaPixels = kReduceThreads * kReducePixelsPerThread;  // 1024 contiguous pixels per CTA
+constexpr int kHalfThreads = kReduceThreads / 2;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+// One CTA's partial sums over pixels [cta*1024, cta*1024+1024) of a level.
+// The reference frame's vertices, normals and intensities of the tile (36 KB)
+// are staged in shared memory with asynchronous 16-byte copies issued by all
+// threads at once, so each pixel then waits for a single round trip: the
+// gather of the current frame at its projection.  Warps 0-3 accumulate ICP
+// rows, warps 4-7 photometric rows (29 sums per thread), each thread 8 pixels
+// 128 apart; warp shuffle tree, then a fixed-order pass over the four warps of
+// each half.  Writes 58 floats to part.
+__device__ __forceinline__ void cta_partial(const SessionView &sv, int level, int rs, int cs, const M34 &T,
+                                            float stddev, int cta, float *part) {
+    __shared__ float warp_sums[kReduceThreads / 32][29];
+    __shared__ __align__(16) float4 s_v[kCtaPixels];
+    __shared__ __align__(16) float4 s_n[kCtaPixels];
+    __shared__ __align__(16) float s_i[kCtaPixels];
+    const PhotoConst pc = photo_const(stddev);
+    const int P = sv.lv[level].w * sv.lv[level].h;
+    const int first = cta * kCtaPixels;
+    const int n = min(kCtaPixels, P - first);
+    {
+        const float4 *gv = sv.vmap[rs][level] + first, *gn = sv.nmap[rs][level] + first;
+        const float *gi = sv.inten[rs][level] + first;
+        for (int c = threadIdx.x; c < n; c += kReduceThreads) {
+            cp_async16(&s_v[c], gv + c);
+            cp_async16(&s_n[c], gn + c);
+        }
+        // intensities in 16-byte chunks; the last chunk may run up to 3 floats past
+        // the image, inside the image's 256-byte-rounded allocation
+        for (int c = threadIdx.x; c < (n + 3) / 4; c += kReduceThreads) cp_async16(&s_i[4 * c], gi + 4 * c);
+        asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
+    }
+    __syncthreads();
+    const int half = threadIdx.x / kHalfThreads, t = threadIdx.x % kHalfThreads;
+    float acc[29];
+#pragma unroll
+    for (int k = 0; k < 29; ++k) acc[k] = 0.f;
+#pragma unroll 2
+    for (int i = 0; i < kCtaPixels / kHalfThreads; ++i) {
+        const int c = t + i * kHalfThreads;
+        if (c >= n) break;
+        float row[7];
+        const bool ok = half == 0 ? icp_row(sv, level, cs, T, s_v[c], s_n[c], row)
+                                  : rgb_row(sv, level, cs, T, pc, s_v[c], s_i[c], row);
+        if (ok) accumulate(acc, row);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < 29; ++k) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 29; ++k) warp_sums[wid][k] = acc[k];
+    __syncthreads();
+    if (lane < 29 && (wid == 0 || wid == 4)) {
+        float s = 0.f;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) s += warp_sums[wid + w][lane];
+        part[(wid == 0 ? 0 : 29) + lane] = s;
+    }
+}
+
+// Sum of the n partial records in FP64: 4 groups of 64 threads take every
+// fourth record in order, then the 4 group sums are added in order.
+__device__ __forceinline__ void sum_partials(const float *parts, int n, double *total) {
+    __shared__ double grp[4][kPartialStride];
+    const int g = threadIdx.x >> 6, k = threadIdx.x & 63;
+    if (k < kReduceWidth) {
+        double s = 0.0;
+#pragma unroll 4
+        for (int c = g; c < n; c += 4) s += (double)__ldcg(parts + (size_t)c * kPartialStride + k);
+        grp[g][k] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < kReduceWidth)
+        total[threadIdx.x] = ((grp[0][threadIdx.x] + grp[1][threadIdx.x]) + grp[2][threadIdx.x]) + grp[3][threadIdx.x];
+    __syncthreads();
+}
+
 struct ReduceArgs {
     int level, iter, once;
     float pose[12];
@@ -221,7 +323,7 @@ struct ReduceArgs {
 
 __device__ void gn_epilogue(const SessionView &sv, int level, int iter, const double *s);
 
-__global__ void __launch_bounds__(kReduceThreads) gn_reduce_kernel(const SessionView *svs, ReduceArgs a) {
+__global__ void __launch_bounds__(kReduceThreads, 3) gn_reduce_kernel(const SessionView *svs, ReduceArgs a) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     TrackState *ts = sv.ts;
@@ -245,36 +347,7 @@ __global__ void __launch_bounds__(kReduceThreads) gn_reduce_kernel(const Session
     }
     __syncthreads();
     const int rs = ts->idx, cs = 1 - ts->idx;
-    const int P = sv.lv[level].w * sv.lv[level].h;
-    const float stddev = stddev_s;
-
-    float acc[kReduceWidth];
-#pragma unroll
-    for (int k = 0; k < kReduceWidth; ++k) acc[k] = 0.f;
-    const int stride = sv.red_ctas[level] * kReduceThreads;
-    for (int p = blockIdx.x * kReduceThreads + threadIdx.x; p < P; p += stride) {
-        float row[7];
-        if (icp_row(sv, level, rs, cs, T, p, row)) accumulate(acc, row);
-        if (rgb_row(sv, level, rs, cs, T, stddev, p, row)) accumulate(acc + 29, row);
-    }
-    // BlockReduce (reduce_sum.h:11-46): warp shuffle tree, then across warps
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-        for (int k = 0; k < kReduceWidth; ++k) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
-    __shared__ float warp_sums[kReduceThreads / 32][kReduceWidth];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < kReduceWidth; ++k) warp_sums[wid][k] = acc[k];
-    __syncthreads();
-    float *part = sv.partials + (size_t)blockIdx.x * kPartialStride;
-    if (threadIdx.x < kReduceWidth) {
-        float s = 0.f;
-#pragma unroll
-        for (int w = 0; w < kReduceThreads / 32; ++w) s += warp_sums[w][threadIdx.x];
-        part[threadIdx.x] = s;
-    }
+    cta_partial(sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.partials + (size_t)blockIdx.x * kPartialStride);
     // last CTA of this session finishes the reduction and takes the step
     __threadfence();
     __syncthreads();
@@ -284,13 +357,8 @@ __global__ void __launch_bounds__(kReduceThreads) gn_reduce_kernel(const Session
     if (ticket != (unsigned)sv.red_ctas[level] - 1u) return;
     __threadfence();
     __shared__ double total[kReduceWidth];
-    if (threadIdx.x < kReduceWidth) {
-        double s = 0.0;
-        for (int c = 0; c < sv.red_ctas[level]; ++c) s += (double)__ldcg(sv.partials + (size_t)c * kPartialStride + threadIdx.x);
-        total[threadIdx.x] = s;
-        ts->last_sums[threadIdx.x] = s;
-    }
-    __syncthreads();
+    sum_partials(sv.partials, sv.red_ctas[level], total);
+    if (threadIdx.x < kReduceWidth) ts->last_sums[threadIdx.x] = total[threadIdx.x];
     if (threadIdx.x == 0) {
         sv.ctr[C_TICKET] = 0;
         if (!a.once) gn_epilogue(sv, level, a.iter, total);
@@ -434,6 +502,7 @@ __global__ void track_finish_kernel(const SessionView *svs, int frame_mode) {
         ts->idx = 1 - ts->idx;
         ts->has_ref = 1;
         pose_copy(ts->pose, ts->map_pose);
+        update_map_floats(ts);
         ts->frame_index += 1;
     }
 }
@@ -491,41 +560,15 @@ constexpr int kStaticTicketSlot = kStaticReduceCtas * kPartialStride;
 // partial records of kStaticReduceCtas CTAs, then the ticket (as unsigned bits)
 static __device__ __align__(256) float g_reduce_scratch[kStaticTicketSlot + 64];
 
-__global__ void __launch_bounds__(kReduceThreads) reduce_static_kernel(SessionView sv, ReduceArgs a, float *scratch,
-                                                                       double *out) {
-    const int level = 0, rs = 0, cs = 1;
+__global__ void __launch_bounds__(kReduceThreads, 3) reduce_static_kernel(SessionView sv, ReduceArgs a,
+                                                                          float *scratch, double *out) {
     const int nctas = sv.red_ctas[0];
     __shared__ M34 T;
     if (threadIdx.x == 0)
 #pragma unroll
         for (int i = 0; i < 12; ++i) T.m[i] = a.pose[i];
     __syncthreads();
-    const int P = sv.lv[0].w * sv.lv[0].h;
-    float acc[kReduceWidth];
-#pragma unroll
-    for (int k = 0; k < kReduceWidth; ++k) acc[k] = 0.f;
-    const int stride = nctas * kReduceThreads;
-    for (int p = blockIdx.x * kReduceThreads + threadIdx.x; p < P; p += stride) {
-        float row[7];
-        if (icp_row(sv, level, rs, cs, T, p, row)) accumulate(acc, row);
-        if (rgb_row(sv, level, rs, cs, T, a.stddev, p, row)) accumulate(acc + 29, row);
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-        for (int k = 0; k < kReduceWidth; ++k) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
-    __shared__ float warp_sums[kReduceThreads / 32][kReduceWidth];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < kReduceWidth; ++k) warp_sums[wid][k] = acc[k];
-    __syncthreads();
-    if (threadIdx.x < kReduceWidth) {
-        float s = 0.f;
-#pragma unroll
-        for (int w = 0; w < kReduceThreads / 32; ++w) s += warp_sums[w][threadIdx.x];
-        scratch[(size_t)blockIdx.x * kPartialStride + threadIdx.x] = s;
-    }
+    cta_partial(sv, 0, 0, 1, T, a.stddev, blockIdx.x, scratch + (size_t)blockIdx.x * kPartialStride);
     __threadfence();
     __syncthreads();
     __shared__ unsigned int ticket;
@@ -534,11 +577,9 @@ __global__ void __launch_bounds__(kReduceThreads) reduce_static_kernel(SessionVi
     __syncthreads();
     if (ticket != (unsigned)nctas - 1u) return;
     __threadfence();
-    if (threadIdx.x < kReduceWidth) {
-        double s = 0.0;
-        for (int c = 0; c < nctas; ++c) s += (double)__ldcg(scratch + (size_t)c * kPartialStride + threadIdx.x);
-        out[threadIdx.x] = s;
-    }
+    __shared__ double total[kReduceWidth];
+    sum_partials(scratch, nctas, total);
+    if (threadIdx.x < kReduceWidth) out[threadIdx.x] = total[threadIdx.x];
     if (threadIdx.x == 0) *tk = 0u;
 }
 

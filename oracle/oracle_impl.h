@@ -203,7 +203,9 @@ static inline R vox_w(const MAP *m, size_t v) {
     return m->w[v];
 #else
     if (m->cfg.voxel_layout == 0) return m->wf[v];
-    return (float)m->w16[v] * (1.0f / 256.f);
+    _Float16 h;
+    memcpy(&h, &m->w16[v], 2);
+    return (float)h;
 #endif
 }
 static inline void vox_store(MAP *m, size_t v, R sdf, R w) {
@@ -217,9 +219,8 @@ static inline void vox_store(MAP *m, size_t v, R sdf, R w) {
     } else {
         _Float16 h = (_Float16)sdf;
         memcpy(&m->sdf[v], &h, 2);
-        float q = w * 256.f + 0.5f;
-        if (!(q < 65280.f)) q = 65280.f;
-        m->w16[v] = (uint16_t)or_trunc_sat(q);
+        _Float16 hw = (_Float16)(w > 255.f ? 255.f : w);
+        memcpy(&m->w16[v], &hw, 2);
     }
 #endif
 }
