@@ -41,11 +41,12 @@ VOXELS = (0.005, 0.006, 0.008, 0.01)  # served sessions draw voxel sizes of 5-10
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--sessions", type=int, default=64)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--plain-frames", type=int, default=48)
+    ap.add_argument("--plain-frames", type=int, default=0,
+                    help="timed frames per plain session (0 = as many as the timed ticks)")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
@@ -147,21 +148,28 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def kernel_bytes(L, sessions, phase: str, K) -> float:
-    """Algorithmic bytes of one launch of the phase's kernel, summed over sessions."""
-    P = K.width * K.height
-    total = 0.0
+def work_counters(sessions) -> tuple[int, int]:
+    """Cumulative (pixel-iterations, integrated blocks) summed over sessions."""
+    pi = ib = 0
     for s in sessions:
         st = s.stats()
-        sv = 8 if s.cfg.voxel_layout == L.VOXEL_HALF else 12
-        if phase == "integrate":
-            # voxel read-modify-write of every visible block + per-pixel depth/weight and colour
-            total += 2.0 * sv * 512 * st.visible_blocks + P * (8 + 4)
-        elif phase == "track":
-            # fused ICP + photometric rows: ref vmap/nmap/intensity + cur vmap/nmap/I/dI per pixel-iteration
-            its = sum(s.cfg.max_iterations[l] * (P >> (2 * l)) for l in range(s.cfg.num_levels))
-            total += 80.0 * its
-    return total
+        pi += st.pixel_iterations
+        ib += st.integrated_blocks
+    return pi, ib
+
+
+def kernel_bytes(L, sessions, phase: str, K, d_pixel_iters: int, d_blocks: int, ticks: int) -> float:
+    """Algorithmic bytes per tick of the phase's kernel, from the work the
+    sessions actually did during the timed ticks (iterations that the
+    reference's early-exit rules skipped read nothing)."""
+    P = K.width * K.height
+    sv = 8 if sessions[0].cfg.voxel_layout == L.VOXEL_HALF else 12
+    if phase == "integrate":
+        # voxel read-modify-write of every visible block + per-pixel depth/weight and colour
+        return (2.0 * sv * 512 * d_blocks + len(sessions) * ticks * P * (8 + 4)) / ticks
+    # fused ICP + photometric rows: reference vertex+normal (32 B) and intensity (4 B),
+    # current vertex+normal (32 B) and intensity + gradients (12 B) per pixel-iteration
+    return 80.0 * d_pixel_iters / ticks
 
 
 # ----------------------------------------------------------------------------- replicas
@@ -346,10 +354,12 @@ def run_ours(args):
 
     # ---- per-phase kernel times: the same ticks launched directly on the stream
     # with CUDA events at the phase boundaries (a second timed region, no graph)
+    pi0, ib0 = work_counters(sessions)
     batch.set_timing(True)
     for k in range(n_phase):
         tick(warm + steps + k, graph=False)
     phases = batch.phase_ms()
+    pi1, ib1 = work_counters(sessions)
     batch.set_timing(False)
     torch.cuda.synchronize()
 
@@ -360,18 +370,21 @@ def run_ours(args):
     # roofline of the dominant kernel phase
     dom = max(("integrate", "track"), key=lambda n: phases[n])
     peak, peak_kind = measured_peaks()
-    bytes_launch = kernel_bytes(L, sessions, dom, K)
+    bytes_launch = kernel_bytes(L, sessions, dom, K, pi1 - pi0, ib1 - ib0, phases["ticks"])
     n_launch = 1 if dom == "integrate" else sum(sessions[0].cfg.max_iterations[l] for l in range(3))
     achieved = bytes_launch / (phases[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": None, "kernel": "integrate_kernel" if dom == "integrate" else "gn_reduce_kernel",
                 "launches_per_step": n_launch, "peak_source": f"{peak_kind} hbm_gbs",
                 "algorithmic_bytes_per_step": bytes_launch,
+                "work_per_step": {"pixel_iterations": (pi1 - pi0) / phases["ticks"],
+                                  "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
                 "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream"}
 
-    # ---- end to end through the public API with host buffers (pinned)
+    # ---- end to end through the public API with host buffers (pinned): the same
+    # frames as the timed ticks, after the same warm-up frames (untimed)
     n_e2e = min(steps, 10)
-    host = [(frames[i][0][warm:warm + n_e2e].cpu().pin_memory(), frames[i][1][warm:warm + n_e2e].cpu().pin_memory())
+    host = [(frames[i][0][:warm + n_e2e].cpu().pin_memory(), frames[i][1][:warm + n_e2e].cpu().pin_memory())
             for i in range(S)]
     e2e_sessions = [L.System(K, session_config(L, i)) for i in range(S)]
     for i, s in enumerate(e2e_sessions):
@@ -379,22 +392,28 @@ def run_ours(args):
     eb = L.FusionBatch(S)
     for i, s in enumerate(e2e_sessions):
         eb.set(i, s)
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    for k in range(n_e2e):
+
+    def e2e_tick(k):
         for i, s in enumerate(e2e_sessions):
             s.stage(host[i][0][k], host[i][1][k])
         eb.process(active, use_graph=use_graph)
         for s in e2e_sessions:
             s.get_pose()  # result read-back (synchronises)
+
+    for k in range(warm):
+        e2e_tick(k)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(warm, warm + n_e2e):
+        e2e_tick(k)
     t1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = t0.elapsed_time(t1)
     e2e = {"value": S * world * n_e2e / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": S * W * H * 5,
            "d2h_bytes_per_step": S * 16 * 8, "steps": n_e2e,
-           "note": "first ticks of fresh sessions, graph capture included"}
+           "note": f"frames {warm}..{warm + n_e2e - 1} of every session after {warm} untimed warm-up frames"}
     eb.close()
     del e2e_sessions
 
@@ -402,9 +421,12 @@ def run_ours(args):
     plain_sessions = [L.System(K, session_config(L, i)) for i in range(min(S, 8))]
     for i, s in enumerate(plain_sessions):
         s.set_pose(poses0[i])
-    nplain = args.plain_frames
-    per = max(1, nplain // len(plain_sessions))
+    per = max(1, min(args.plain_frames or steps, nfr - warm))
     plat = []
+    for k in range(warm):  # the served sessions' warm-up frames, untimed
+        for i, s in enumerate(plain_sessions):
+            d, c = frames[i]
+            s.process_images(d[k], c[k])
     torch.cuda.synchronize()
     tp = time.perf_counter()
     for k in range(per):
@@ -413,7 +435,7 @@ def run_ours(args):
             b = torch.cuda.Event(enable_timing=True)
             a.record(stream)
             d, c = frames[i]
-            s.process_images(d[k], c[k])
+            s.process_images(d[warm + k], c[warm + k])
             b.record(stream)
             s.get_pose()
             plat.append(a.elapsed_time(b))
@@ -424,7 +446,8 @@ def run_ours(args):
     plat.sort()
     plain = {"value": plain_fps, "unit": UNIT, "frames": nplain_done, "sessions": len(plain_sessions),
              "p50_ms": plat[len(plat) // 2], "p99_ms": plat[min(len(plat) - 1, int(0.99 * len(plat)))],
-             "path": "gbf_process_frame per session, direct launches, pose read back per frame"}
+             "path": "gbf_process_frame per session, direct launches, pose read back per frame",
+             "frame_indices": f"{warm}..{warm + per - 1} after {warm} untimed warm-up frames"}
     del plain_sessions
 
     if rank != 0:

@@ -20,7 +20,8 @@
  *   DenseMapping::raycast                  src/voxel_hashing/voxel_hashing.cpp:87-119 -> gbf_raycast
  *   DenseMapping::reset_mapping            src/voxel_hashing/voxel_hashing.cpp:137-140 -> gbf_session_reset
  *   DenseMapping::fetch_mesh_*             src/voxel_hashing/voxel_hashing.cpp:142-187 -> gbf_extract_mesh
- *   DenseMapping::write/readMapFromDisk    src/voxel_hashing/voxel_hashing.cpp:189-205 -> gbf_map_export / gbf_map_import
+ *   DenseMapping::write/readMapFromDisk    src/voxel_hashing/voxel_hashing.cpp:189-205 -> gbf_map_write_dump / gbf_map_read_dump
+ *   MapStruct::writeToDisk/readFromDisk    src/data_struct/map_struct.cu:535-613      -> gbf_dump_write / gbf_dump_read
  *   DeviceImage::upload                    src/tracking/device_image.cpp:146-181      -> gbf_build_pyramid
  *   DenseTracking::compute_transform       src/tracking/icp_tracker.cpp:23-156        -> gbf_track
  *   icp_reduce / rgb_step                  src/tracking/pose_estimator.cu:267-307,
@@ -53,7 +54,9 @@ typedef enum gbf_status {
     GBF_ERR_CUDA = 2,         /* a CUDA runtime call failed                   */
     GBF_ERR_OUT_OF_MEMORY = 3,/* device allocation failed                     */
     GBF_ERR_CAPACITY = 4,     /* batch slot / output buffer too small         */
-    GBF_ERR_NO_DEVICE = 5     /* no CUDA device visible                       */
+    GBF_ERR_NO_DEVICE = 5,    /* no CUDA device visible                       */
+    GBF_ERR_IO = 6            /* a file could not be opened, read or written, or
+                                 its contents are not a valid map dump          */
 } gbf_status;
 
 /* Per-session device status bits (sticky until gbf_session_reset). */
@@ -117,6 +120,9 @@ typedef struct gbf_frame_stats {
     int32_t render_blocks_valid;
     uint32_t status;      /* GBF_FLAG_* bits                                      */
     gbf_track_result track;
+    int32_t level_iterations[GBF_MAX_LEVELS]; /* last tracking, per level          */
+    int64_t pixel_iterations;  /* cumulative pixels x Gauss-Newton iterations     */
+    int64_t integrated_blocks; /* cumulative visible blocks integrated            */
 } gbf_frame_stats;
 
 typedef struct gbf_session gbf_session;
@@ -223,6 +229,53 @@ GBF_API gbf_status gbf_map_export(gbf_session *s, int32_t *coords, float *sdf, f
                                   int64_t max_blocks, int64_t *n_blocks);
 GBF_API gbf_status gbf_map_import(gbf_session *s, const int32_t *coords, const float *sdf, const float *weight,
                                   const uint8_t *rgb, int64_t n_blocks);
+/* ---- map dump in the reference's raw layout ------------------------------------ */
+/* MapSize (include/data_struct/map_struct.h:53-58): the three sizes a dump is
+ * laid out with.  The reference's own writer always uses its MapState
+ * defaults (src/data_struct/map_struct.cu:19-21): 200000 blocks, 250000 hash
+ * entries (200000 buckets + 50000 excess). */
+typedef struct gbf_map_size {
+    int32_t num_blocks;
+    int32_t num_hash_entries;
+    int32_t num_buckets;
+} gbf_map_size;
+
+/* File layout, as MapStruct::writeToDisk writes it (src/data_struct/map_struct.cu:535-573):
+ *   Voxel[num_blocks*512]      12 B: int16 sdf (x32767, truncated), 2 pad, float weight,
+ *                              uint8 rgb[3], 1 pad           (include/data_struct/voxel.h:20-22)
+ *   HashEntry[num_hash_entries] 20 B: int32 ptr (block id * 512, -1 empty), int32 offset
+ *                              (1-based excess link), int32 pos[3] (include/data_struct/hash_entry.h:20-22)
+ *   int32 heap[num_blocks], int32 bucket_mutex[num_buckets], int32 heap_counter, int32 excess_counter
+ * and "<path>.txt" holds the MapSize as three raw int32.
+ *
+ * gbf_dump_write / gbf_dump_read are host-only (no device, no session): they
+ * convert between that layout and the canonical per-block arrays of
+ * gbf_map_export / gbf_map_import.  The writer lays blocks out as the
+ * reference's single-threaded createBlock (map_struct.cu:280-323) would after
+ * inserting them in the given order: block i at ptr i*512, home bucket
+ * computeHash(pos, num_buckets) when free, else appended to that bucket's
+ * excess chain with offsets 1, 2, ... in insertion order; the heap and its
+ * counter as after i pops; excess_counter = the next free offset.  (The
+ * reference's first excess insert takes offset 0, which links nothing and
+ * lands on bucket num_buckets-1; the writer does not reproduce that.)
+ * The reader takes every entry with ptr != -1, in table order, as the
+ * reference's visibility pass does (src/voxel_hashing/depth_fusion.cu:49-93);
+ * a position seen twice keeps its first entry.  sdf = int16 / 32767.f. */
+GBF_API gbf_status gbf_dump_write(const char *path, const gbf_map_size *size, const int32_t *coords,
+                                  const float *sdf, const float *weight, const uint8_t *rgb, int64_t n_blocks);
+/* With coords == NULL only *size and *n_blocks are filled. */
+GBF_API gbf_status gbf_dump_read(const char *path, gbf_map_size *size, int32_t *coords, float *sdf, float *weight,
+                                 uint8_t *rgb, int64_t max_blocks, int64_t *n_blocks);
+/* DenseMapping::writeMapToDisk (src/voxel_hashing/voxel_hashing.cpp:189-196): the
+ * session's allocated blocks, in block-id order, through gbf_dump_write.
+ * size NULL = the reference's default sizes.  Synchronises. */
+GBF_API gbf_status gbf_map_write_dump(gbf_session *s, const char *path, const gbf_map_size *size);
+/* DenseMapping::readMapFromDisk (src/voxel_hashing/voxel_hashing.cpp:198-205): replaces
+ * the session's map with the dump's blocks; the camera pose and tracking state
+ * are kept, as in the reference, which uploads only the map storage.
+ * Synchronises. */
+GBF_API gbf_status gbf_map_read_dump(gbf_session *s, const char *path);
+
 /* Visible-block list of the last fuse (block coordinates), synchronises. */
 GBF_API gbf_status gbf_visible_blocks(gbf_session *s, int32_t *coords, int64_t max_blocks, int64_t *n_blocks);
 /* z-range grid of the last raycast: 2 floats per cell (min, max), (H/8)x(W/8). */

@@ -128,6 +128,13 @@ class DenseMapping : public Session {
               "fetch_mesh_with_colour");
         return (size_t)n;
     }
+    // the reference's raw dump: file_name + file_name.txt (reference default sizes)
+    void writeMapToDisk(const std::string &file_name) {
+        check(gbf_map_write_dump(handle(), file_name.c_str(), nullptr), "writeMapToDisk");
+    }
+    void readMapFromDisk(const std::string &file_name) {
+        check(gbf_map_read_dump(handle(), file_name.c_str()), "readMapFromDisk");
+    }
 };
 
 class DenseTracking : public DenseMapping {

@@ -27,6 +27,7 @@ from ._lib import (FLAG_COORD_RANGE, FLAG_HASH_FULL, FLAG_NAN_POSE, FLAG_POOL_EX
 
 __all__ = [
     "IntrinsicMatrix", "DenseMapping", "DenseTracking", "System", "FusionBatch", "SynthScene", "TrackingResult",
+    "write_dump", "read_dump",
     "default_config", "session_bytes", "GbfError", "VOXEL_REF", "VOXEL_HALF", "MESH_VERTEX", "MESH_NORMAL",
     "MESH_COLOUR", "FLAG_POOL_EXHAUSTED", "FLAG_HASH_FULL", "FLAG_COORD_RANGE", "FLAG_TRACK_FAILED",
     "FLAG_NAN_POSE", "version",
@@ -205,16 +206,18 @@ class DenseMapping(_Session):
         call("gbf_map_import", self._h, coords.ctypes.data, sdf.ctypes.data, w.ctypes.data, rgb.ctypes.data,
              len(coords))
 
-    def writeMapToDisk(self, file_name: str) -> None:
-        """Session snapshot (compact: allocated blocks only) as .npz."""
-        coords, sdf, w, rgb = self.export()
-        np.savez_compressed(file_name, coords=coords, sdf=sdf, weight=w, rgb=rgb,
-                            voxel_size=self.cfg.voxel_size, pose=self.get_pose())
+    def writeMapToDisk(self, file_name: str, size: tuple[int, int, int] | None = None) -> None:
+        """DenseMapping::writeMapToDisk (src/voxel_hashing/voxel_hashing.cpp:189-196): the
+        reference's raw dump (``file_name`` + ``file_name.txt``).  ``size`` =
+        (num_blocks, num_hash_entries, num_buckets); None = the reference's
+        defaults, which its own reader assumes."""
+        ms = None if size is None else C.byref(_lib.MapSize(*size))
+        call("gbf_map_write_dump", self._h, str(file_name).encode(), ms)
 
     def readMapFromDisk(self, file_name: str) -> None:
-        d = np.load(file_name if file_name.endswith(".npz") else file_name + ".npz")
-        self.reset()
-        self.import_blocks(d["coords"], d["sdf"], d["weight"], d["rgb"])
+        """DenseMapping::readMapFromDisk (src/voxel_hashing/voxel_hashing.cpp:198-205):
+        replaces the map with the dump's blocks; pose and tracking state stay."""
+        call("gbf_map_read_dump", self._h, str(file_name).encode())
 
     def visible_blocks(self) -> np.ndarray:
         n = C.c_int64()
@@ -330,6 +333,34 @@ class FusionBatch:
             self.close()
         except Exception:
             pass
+
+
+def write_dump(file_name: str, coords, sdf, weight, rgb, size: tuple[int, int, int] | None = None) -> None:
+    """Reference raw map dump from canonical per-block arrays (host only, no device)."""
+    coords = np.ascontiguousarray(coords, np.int32).reshape(-1, 3)
+    n = len(coords)
+    sdf = np.ascontiguousarray(sdf, np.float32).reshape(n, 512)
+    weight = np.ascontiguousarray(weight, np.float32).reshape(n, 512)
+    rgb = np.ascontiguousarray(rgb, np.uint8).reshape(n, 512, 3)
+    ms = None if size is None else C.byref(_lib.MapSize(*size))
+    call("gbf_dump_write", str(file_name).encode(), ms, coords.ctypes.data, sdf.ctypes.data, weight.ctypes.data,
+         rgb.ctypes.data, n)
+
+
+def read_dump(file_name: str):
+    """Blocks of a reference raw map dump (host only): (coords, sdf, weight, rgb, size)."""
+    ms = _lib.MapSize()
+    n = C.c_int64()
+    call("gbf_dump_read", str(file_name).encode(), C.byref(ms), None, None, None, None, 0, C.byref(n))
+    k = int(n.value)
+    coords = np.zeros((k, 3), np.int32)
+    sdf = np.zeros((k, 512), np.float32)
+    w = np.zeros((k, 512), np.float32)
+    rgb = np.zeros((k, 512, 3), np.uint8)
+    if k:
+        call("gbf_dump_read", str(file_name).encode(), None, coords.ctypes.data, sdf.ctypes.data, w.ctypes.data,
+             rgb.ctypes.data, k, C.byref(n))
+    return coords, sdf, w, rgb, (ms.num_blocks, ms.num_hash_entries, ms.num_buckets)
 
 
 class SynthScene:

@@ -13,7 +13,7 @@ LIB_PATH = _PKG / "_build" / "libgbfusion.so"
 
 MAX_LEVELS = 5
 OK = 0
-STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "OUT_OF_MEMORY", 4: "CAPACITY", 5: "NO_DEVICE"}
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "OUT_OF_MEMORY", 4: "CAPACITY", 5: "NO_DEVICE", 6: "IO"}
 
 FLAG_POOL_EXHAUSTED = 1
 FLAG_HASH_FULL = 2
@@ -52,7 +52,9 @@ class TrackResult(C.Structure):
 
 class FrameStats(C.Structure):
     _fields_ = [("frame_index", C.c_int64), ("allocated_blocks", C.c_int32), ("visible_blocks", C.c_int32),
-                ("render_blocks_valid", C.c_int32), ("status", C.c_uint32), ("track", TrackResult)]
+                ("render_blocks_valid", C.c_int32), ("status", C.c_uint32), ("track", TrackResult),
+                ("level_iterations", C.c_int32 * MAX_LEVELS), ("pixel_iterations", C.c_int64),
+                ("integrated_blocks", C.c_int64)]
 
 
 class ReduceInputs(C.Structure):
@@ -62,6 +64,11 @@ class ReduceInputs(C.Structure):
                 ("cur_vmap", C.c_void_p), ("cur_nmap", C.c_void_p), ("cur_intensity", C.c_void_p),
                 ("cur_didx", C.c_void_p), ("cur_didy", C.c_void_p),
                 ("dist_thresh", C.c_float), ("angle_thresh", C.c_float)]
+
+
+class MapSize(C.Structure):
+    """MapSize (include/data_struct/map_struct.h:53-58)."""
+    _fields_ = [("num_blocks", C.c_int32), ("num_hash_entries", C.c_int32), ("num_buckets", C.c_int32)]
 
 
 class SynthParams(C.Structure):
@@ -103,6 +110,10 @@ SIGNATURES = {
     "gbf_process_frame_staged": (C.c_int, [_P, _P]),
     "gbf_map_export": (C.c_int, [_P, _P, _P, _P, _P, _I64, C.POINTER(C.c_int64)]),
     "gbf_map_import": (C.c_int, [_P, _P, _P, _P, _P, _I64]),
+    "gbf_dump_write": (C.c_int, [C.c_char_p, _P, _P, _P, _P, _P, _I64]),
+    "gbf_dump_read": (C.c_int, [C.c_char_p, _P, _P, _P, _P, _P, _I64, C.POINTER(C.c_int64)]),
+    "gbf_map_write_dump": (C.c_int, [_P, C.c_char_p, _P]),
+    "gbf_map_read_dump": (C.c_int, [_P, C.c_char_p]),
     "gbf_visible_blocks": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_int64)]),
     "gbf_zrange": (C.c_int, [_P, _P, _I64]),
     "gbf_batch_create": (C.c_int, [_I32, C.POINTER(_P)]),

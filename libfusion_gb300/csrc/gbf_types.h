@@ -74,6 +74,9 @@ struct TrackState {
     int tracking;          // this frame runs Gauss-Newton
     float icp_inliers, rgb_inliers;
     long long frame_index;
+    long long pixel_iterations;   // cumulative pixels reduced by Gauss-Newton iterations
+    long long integrated_blocks;  // cumulative visible blocks integrated
+    int level_iters[kMaxLevels];  // iterations run per level in the last tracking
     double last_sums[kReduceWidth];
 };
 

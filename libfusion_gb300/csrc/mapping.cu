@@ -216,8 +216,10 @@ __global__ void visible_kernel(const SessionView *svs) {
     }
 }
 
+constexpr int kIntThreads = 128;  // threads per integration CTA (512 / kIntThreads voxels each)
+
 template <int LAYOUT>
-__global__ void __launch_bounds__(256) integrate_kernel(const SessionView *svs, int mode) {
+__global__ void __launch_bounds__(kIntThreads) integrate_kernel(const SessionView *svs, int mode) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || sv.layout != LAYOUT) return;
     __shared__ M34 Tcw;
@@ -226,6 +228,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(const SessionView *svs, 
     const LevelK &K = sv.lv[0];
     const int W = K.w, H = K.h;
     const int nvis = sv.ctr[C_NVIS];
+    if (blockIdx.x == 0 && threadIdx.x == 0) sv.ts->integrated_blocks += nvis;
     const float voxel = sv.voxel, tau = sv.tau, inv_tau = sv.inv_tau;
 
     for (int b = blockIdx.x; b < nvis; b += gridDim.x) {
@@ -234,8 +237,8 @@ __global__ void __launch_bounds__(256) integrate_kernel(const SessionView *svs, 
         const bool fresh = tagged < 0;
         const int4 bc = sv.bcoord[id];
 #pragma unroll
-        for (int half_i = 0; half_i < 2; ++half_i) {
-            const int li = threadIdx.x + half_i * 256;
+        for (int half_i = 0; half_i < kBlockVoxels / kIntThreads; ++half_i) {
+            const int li = threadIdx.x + half_i * kIntThreads;
             const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
             const size_t vi = (size_t)id * kBlockVoxels + li;
             const float3 p = Tcw.apply((float)(bc.x * 8 + lx) * voxel, (float)(bc.y * 8 + ly) * voxel,
@@ -310,8 +313,8 @@ void launch_integrate(const SessionView *d_sv, int nslots, const Extent &ex, int
     if (mode != 1) fuse_prep_kernel<<<dim3((ex.w * ex.h + 255) / 256, nslots), 256, 0, st>>>(d_sv, mode);
     // one CTA per visible block, grid-stride; 8 resident CTAs of 256 threads per SM
     const int gi = 152 * 8;
-    if (layouts[GBF_VOXEL_REF]) integrate_kernel<GBF_VOXEL_REF><<<dim3(gi, nslots), 256, 0, st>>>(d_sv, mode);
-    if (layouts[GBF_VOXEL_HALF]) integrate_kernel<GBF_VOXEL_HALF><<<dim3(gi, nslots), 256, 0, st>>>(d_sv, mode);
+    if (layouts[GBF_VOXEL_REF]) integrate_kernel<GBF_VOXEL_REF><<<dim3(gi, nslots), kIntThreads, 0, st>>>(d_sv, mode);
+    if (layouts[GBF_VOXEL_HALF]) integrate_kernel<GBF_VOXEL_HALF><<<dim3(gi, nslots), kIntThreads, 0, st>>>(d_sv, mode);
 }
 
 void launch_fuse(const SessionView *d_sv, int nslots, const Extent &ex, int mode, const int *layouts,

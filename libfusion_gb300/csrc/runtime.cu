@@ -213,15 +213,17 @@ TrackState initial_track_state() {
     return t;
 }
 
-gbf_status reset_session(gbf_session *s, cudaStream_t st) {
+gbf_status reset_session(gbf_session *s, cudaStream_t st, bool keep_track = false) {
     reset_table_kernel<<<512, 256, 0, st>>>(s->view.table, s->cfg.num_buckets);
     cudaError_t e = cudaMemsetAsync(s->view.ctr, 0, C_COUNT * sizeof(int), st);
     if (e != cudaSuccess) return cuda_error(e, "reset");
     e = cudaMemsetAsync(s->view.bfresh, 0, (size_t)s->cfg.num_blocks, st);
     if (e != cudaSuccess) return cuda_error(e, "reset");
-    const TrackState t = initial_track_state();
-    e = cudaMemcpyAsync(s->view.ts, &t, sizeof(t), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_error(e, "reset");
+    if (!keep_track) {
+        const TrackState t = initial_track_state();
+        e = cudaMemcpyAsync(s->view.ts, &t, sizeof(t), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_error(e, "reset");
+    }
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "reset");
     return check_cuda("reset");
@@ -288,6 +290,9 @@ int kernels_per_frame(const Extent &ex, const int *layouts) {
 }
 
 }  // namespace
+
+gbf_status reset_map(gbf_session *s) { return reset_session(s, nullptr, true); }
+
 }  // namespace gbf
 
 using namespace gbf;
@@ -530,6 +535,9 @@ GBF_API gbf_status gbf_get_stats(gbf_session *s, gbf_frame_stats *out, void *str
     out->render_blocks_valid = ctr[C_RENDER];
     out->status = (uint32_t)ctr[C_STATUS];
     fill_result(t, &out->track);
+    for (int l = 0; l < GBF_MAX_LEVELS; ++l) out->level_iterations[l] = t.level_iters[l];
+    out->pixel_iterations = t.pixel_iterations;
+    out->integrated_blocks = t.integrated_blocks;
     return GBF_OK;
 }
 

@@ -323,16 +323,26 @@ struct ReduceArgs {
 
 __device__ void gn_epilogue(const SessionView &sv, int level, int iter, const double *s);
 
-__global__ void __launch_bounds__(kReduceThreads, 3) gn_reduce_kernel(const SessionView *svs, ReduceArgs a) {
+// Whether session `sv` runs this (level, iteration): the schedule of
+// compute_transform (icp_tracker.cpp:33-50) with its early `break` per level.
+__device__ __forceinline__ bool session_runs(const SessionView &sv, const ReduceArgs &a) {
+    if (!sv.active || a.level >= sv.levels) return false;
+    if (a.once) return true;
+    const TrackState *ts = sv.ts;
+    if (!ts->tracking || a.iter >= sv.max_iter[a.level]) return false;
+    return !(a.iter > 0 && ts->level_done);
+}
+
+// One CTA per (tile, session): the session's sum over 1024 reference pixels
+// of the ICP and photometric rows; the CTA that completes the session's last
+// tile adds the partials in a fixed order and takes the Gauss-Newton step.
+// Sessions that have left the level, or do not track this frame, return at
+// once.
+__global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const SessionView *svs, ReduceArgs a) {
     const SessionView &sv = svs[blockIdx.y];
-    if (!sv.active) return;
-    TrackState *ts = sv.ts;
     const int level = a.level;
-    if (level >= sv.levels || blockIdx.x >= sv.red_ctas[level]) return;
-    if (!a.once) {
-        if (!ts->tracking || a.iter >= sv.max_iter[level]) return;
-        if (a.iter > 0 && ts->level_done) return;
-    }
+    if (!session_runs(sv, a) || blockIdx.x >= sv.red_ctas[level]) return;
+    TrackState *ts = sv.ts;
     __shared__ M34 T;
     __shared__ float stddev_s;
     if (threadIdx.x == 0) {
@@ -348,7 +358,6 @@ __global__ void __launch_bounds__(kReduceThreads, 3) gn_reduce_kernel(const Sess
     __syncthreads();
     const int rs = ts->idx, cs = 1 - ts->idx;
     cta_partial(sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.partials + (size_t)blockIdx.x * kPartialStride);
-    // last CTA of this session finishes the reduction and takes the step
     __threadfence();
     __syncthreads();
     __shared__ unsigned int ticket;
@@ -396,6 +405,8 @@ __device__ void gn_epilogue(const SessionView &sv, int level, int iter, const do
     pose_copy(ts->est, ts->est_prev);
     pose_copy(next, ts->est);
     ts->iterations += 1;
+    ts->level_iters[level] += 1;
+    ts->pixel_iterations += (long long)sv.lv[level].w * sv.lv[level].h;
     ts->icp_inliers = n_icp;
     ts->rgb_inliers = n_rgb;
 
@@ -458,6 +469,7 @@ __global__ void track_begin_kernel(const SessionView *svs, int frame_mode) {
     pose_identity(ts->est_prev);
     ts->invalid = 0;
     ts->iterations = 0;
+    for (int l = 0; l < kMaxLevels; ++l) ts->level_iters[l] = 0;
     ts->level_done = 0;
     ts->icp_error = FLT_MAX;
     ts->rgb_error = FLT_MAX;

@@ -64,6 +64,7 @@ def lib() -> C.CDLL:
                 f"or_fuse_{s}": (C.c_int, [P, P, P, P, D]),
                 f"or_raycast_{s}": (C.c_int, [P, D, P]),
                 f"or_map_blocks_{s}": (C.c_int64, [P]),
+                f"or_ray_stats_{s}": (None, [P, D, C.POINTER(C.c_longlong), P]),
                 f"or_map_export_{s}": (C.c_int64, [P, P, P, P, P, C.c_int64]),
                 f"or_visible_{s}": (C.c_int64, [P, P, C.c_int64]),
                 f"or_zrange_{s}": (None, [P, P]),
@@ -157,6 +158,16 @@ class OracleMap:
             vmap = np.full((self.K.height, self.K.width, 4), np.nan, np.float32)
         self.fn("or_raycast")(self.h, _d16(pose), _p(vmap))
         return vmap
+
+    def ray_stats(self, pose, per_pixel: bool = False):
+        """March counts of a raycast at `pose` (rays, steps, voxel samples,
+        trilinear reads, hits); with per_pixel, also each pixel's cost in
+        samples (steps + 8 per trilinear read)."""
+        out = (C.c_longlong * 5)()
+        pp = np.zeros((self.K.height, self.K.width), np.int32) if per_pixel else None
+        self.fn("or_ray_stats")(self.h, _d16(pose), out, _p(pp))
+        d = dict(zip(("rays", "steps", "samples", "interps", "hits"), out[:]))
+        return (d, pp) if per_pixel else d
 
     def export(self):
         n = self.fn("or_map_blocks")(self.h)
@@ -285,3 +296,53 @@ class OracleSystem:
             self.fn("or_system_destroy")(self.h)
         except Exception:
             pass
+
+
+# ---- reference raw map dump (MapStruct::writeToDisk, src/data_struct/map_struct.cu:535-573) ----
+
+REF_VOXEL = np.dtype([("sdf", "<i2"), ("pad0", "<i2"), ("weight", "<f4"), ("rgb", "u1", 3), ("pad1", "u1")])
+REF_ENTRY = np.dtype([("ptr", "<i4"), ("offset", "<i4"), ("pos", "<i4", 3)])
+REF_DEFAULT_SIZE = (200000, 250000, 200000)  # MapStruct() defaults, map_struct.cu:19-21
+
+
+def parse_ref_dump(path) -> dict:
+    """The arrays of a raw dump, in writeToDisk's order: voxels (Voxel, voxel.h:20-22),
+    hash table (HashEntry, hash_entry.h:20-22), heap, bucket mutexes, heap counter,
+    excess counter; sizes from "<path>.txt" (MapSize, map_struct.h:53-58)."""
+    path = Path(path)
+    txt = Path(str(path) + ".txt")
+    nb, ne, nbk = (np.fromfile(txt, "<i4", 3).tolist() if txt.exists() else REF_DEFAULT_SIZE)
+    raw = np.fromfile(path, np.uint8)
+    out, off = {"size": (nb, ne, nbk)}, 0
+    for name, dt, cnt in (("voxels", REF_VOXEL, nb * 512), ("table", REF_ENTRY, ne), ("heap", np.dtype("<i4"), nb),
+                          ("mutex", np.dtype("<i4"), nbk), ("heap_counter", np.dtype("<i4"), 1),
+                          ("excess_counter", np.dtype("<i4"), 1)):
+        nbytes = dt.itemsize * cnt
+        out[name] = raw[off:off + nbytes].view(dt)
+        off += nbytes
+    if off != raw.size:
+        raise ValueError(f"dump is {raw.size} bytes, its MapSize implies {off}")
+    return out
+
+
+def ref_compute_hash(x: int, y: int, z: int, n: int) -> int:
+    """computeHash (map_struct.cu:143-148): int32 wraparound products, C remainder, made non-negative."""
+    def i32(v):
+        return ((v + 2**31) % 2**32) - 2**31
+    h = i32(i32(x * 73856093) ^ i32(y * 19349669) ^ i32(z * 83492791))
+    r = abs(h) % n * (1 if h >= 0 else -1)  # C remainder takes the dividend's sign
+    return r + n if r < 0 else r
+
+
+def ref_find_entry(dump: dict, pos) -> int:
+    """findEntry (map_struct.cu:365-380): index of the live entry for block `pos`
+    along its bucket's excess chain, or -1."""
+    table, nbk = dump["table"], dump["size"][2]
+    i = ref_compute_hash(int(pos[0]), int(pos[1]), int(pos[2]), nbk)
+    while True:
+        e = table[i]
+        if e["ptr"] != -1 and tuple(e["pos"]) == tuple(int(p) for p in pos):
+            return i
+        if e["offset"] <= 0:
+            return -1
+        i = nbk + int(e["offset"]) - 1

@@ -481,8 +481,13 @@ static void zrange_pass(MAP *m, const M34 *Tcw) {
     }
 }
 
+/* march statistics for the raycast roofline: samples, trilinear reads, steps, rays */
+typedef struct { long long samples, interps, steps, rays, hits; } RayStats;
+static _Thread_local RayStats *g_rs;
+
 /* read_sdf (ray_tracing.cu:291-305) */
 static R read_sdf(const MAP *m, R px, R py, R pz, int *valid) {
+    if (g_rs) g_rs->samples++;
     const int vx = floor_r(px), vy = floor_r(py), vz = floor_r(pz);
     const int id = map_find(m, vtob(vx), vtob(vy), vtob(vz));
     if (id >= 0) {
@@ -498,6 +503,7 @@ static R read_sdf(const MAP *m, R px, R py, R pz, int *valid) {
 
 /* read_sdf_interped (ray_tracing.cu:307-339) */
 static R read_interp(const MAP *m, R px, R py, R pz, int *valid) {
+    if (g_rs) g_rs->interps++;
     const R fx = px - RFLOOR(px), fy = py - RFLOOR(py), fz = pz - RFLOOR(pz);
     int vp, v;
     R s0, s1, r0, r1, r2, r3;
@@ -544,7 +550,9 @@ static void ray_pixel(const MAP *m, const M34 *Twc, const M34 *Tcw, int x, int y
     V3 r = bs;
     R sdf = 1, last_sdf, step;
     int valid = 0;
+    if (g_rs) g_rs->rays++;
     for (int it = 0; dist_s < dist_e && it < (1 << 16); ++it) {
+        if (g_rs) g_rs->steps++;
         last_sdf = sdf;
         sdf = read_sdf(m, r.x, r.y, r.z, &valid);
         if (sdf <= (R)0.5 && sdf >= (R)-0.5) sdf = read_interp(m, r.x, r.y, r.z, &valid);
@@ -564,6 +572,7 @@ static void ray_pixel(const MAP *m, const M34 *Twc, const M34 *Tcw, int x, int y
         found = valid;
     }
     if (found) {
+        if (g_rs) g_rs->hits++;
         const V3 c = m_apply(Tcw, r.x * m->voxel, r.y * m->voxel, r.z * m->voxel);
         out[0] = (float)c.x; out[1] = (float)c.y; out[2] = (float)c.z; out[3] = 1.0f;
     }
@@ -583,6 +592,28 @@ int SFX(or_raycast)(MAP *m, const double T[16], float *vmap) {
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) ray_pixel(m, &Twc, &Tcw, x, y, vmap + ((size_t)y * W + x) * 4);
     return 1;
+}
+
+/* counts of the last fuse's raycast at pose T (single thread): rays marched,
+ * march steps, voxel samples (each a hash lookup + one voxel read), trilinear
+ * reads, hits */
+void SFX(or_ray_stats)(MAP *m, const double T[16], long long out[5], int32_t *steps_per_pixel) {
+    double inv[12];
+    pose_inv(T, inv);
+    const M34 Twc = to_m(T), Tcw = to_m(inv);
+    zrange_pass(m, &Tcw);
+    RayStats rs = {0, 0, 0, 0, 0};
+    g_rs = &rs;
+    float px[4];
+    if (m->nvis && m->nrender)
+        for (int y = 0; y < m->K.height; ++y)
+            for (int x = 0; x < m->K.width; ++x) {
+                const long long s0 = rs.steps + rs.interps * 8;
+                ray_pixel(m, &Twc, &Tcw, x, y, px);
+                if (steps_per_pixel) steps_per_pixel[y * m->K.width + x] = (int32_t)(rs.steps + rs.interps * 8 - s0);
+            }
+    g_rs = NULL;
+    out[0] = rs.rays; out[1] = rs.steps; out[2] = rs.samples; out[3] = rs.interps; out[4] = rs.hits;
 }
 
 int64_t SFX(or_map_blocks)(const MAP *m) { return m->n_used; }

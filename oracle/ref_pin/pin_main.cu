@@ -4,13 +4,82 @@
 // into oracle/_ref/; never part of the product.
 #include <cstdio>
 #include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
 #include "data_struct/map_struct.h"
 #include "data_struct/intrinsic_matrix.h"
 #include "voxel_hashing/device_tables.h"
 
 using namespace fusion;
 
-int main() {
+// Dump pin: a small chained map filled here, written by the reference's own
+// MapStruct<false>::writeToDisk.  The blocks are laid out as a single-threaded
+// createBlock would insert them in order (home bucket if free, else appended
+// to the bucket's excess chain with offsets 1, 2, ...); the writer under test
+// lays blocks out by the same rule, so its file must match byte for byte.
+// The MapStruct constructors upload the map state to the device, so the host
+// map is built in raw storage and only its host-side members are used.
+static int dump_pin(const char *path) {
+    const int nb = 16, ne = 24, nbk = 8;  // MapSize: blocks, hash entries, buckets
+    const int pos[][3] = {{0, 0, 0},  {1, 0, 0},   {0, 1, 0},  {0, 0, 1},  {-1, -1, -1}, {5, -3, 2},
+                          {-7, 4, 9}, {12, 12, 12}, {-20, 3, 0}, {100, -100, 50}, {3, 3, 3}, {-4, 8, -16}};
+    const int n = sizeof(pos) / sizeof(pos[0]);
+    alignas(MapStruct<false>) static unsigned char raw[sizeof(MapStruct<false>)];
+    MapStruct<false> &m = *reinterpret_cast<MapStruct<false> *>(raw);
+    std::memset(raw, 0, sizeof(raw));
+    m.state.num_total_buckets_ = nbk;
+    m.state.num_total_hash_entries_ = ne;
+    m.state.num_total_voxel_blocks_ = nb;
+    m.size.num_blocks = nb;
+    m.size.num_hash_entries = ne;
+    m.size.num_buckets = nbk;
+    m.create();
+    std::memset((void *)m.map.voxels_, 0, sizeof(Voxel) * nb * BLOCK_SIZE3);
+    for (int i = 0; i < ne; ++i) {
+        m.map.hash_table_[i].ptr_ = -1;
+        m.map.hash_table_[i].offset_ = -1;
+        m.map.hash_table_[i].pos_ = Vector3i(0, 0, 0);
+    }
+    for (int i = 0; i < nb; ++i) m.map.heap_mem_[i] = nb - i - 1;
+    for (int i = 0; i < nbk; ++i) m.map.bucket_mutex_[i] = 0;
+    int next_offset = 1;
+    for (int b = 0; b < n; ++b) {
+        Vector3i p(pos[b][0], pos[b][1], pos[b][2]);
+        int cur = computeHash(p, nbk);
+        HashEntry fresh(p, b * BLOCK_SIZE3, -1);
+        if (m.map.hash_table_[cur].ptr_ == -1) {
+            m.map.hash_table_[cur] = fresh;
+        } else {
+            while (m.map.hash_table_[cur].offset_ > 0) cur = nbk + m.map.hash_table_[cur].offset_ - 1;
+            fresh.offset_ = 0;
+            m.map.hash_table_[nbk + next_offset - 1] = fresh;
+            m.map.hash_table_[cur].offset_ = next_offset++;
+        }
+        for (int i = 0; i < BLOCK_SIZE3; ++i) {
+            Voxel &v = m.map.voxels_[b * BLOCK_SIZE3 + i];
+            v.sdf = (short)(((b * 512 + i) * 37) % 65535 - 32767);
+            v.weight = (float)((b * 7 + i) % 256);
+            v.rgb = Vector3c((unsigned char)((b + i) % 256), (unsigned char)((b * 3 + i) % 256),
+                             (unsigned char)((b * 5 + i) % 256));
+        }
+    }
+    m.map.heap_mem_counter_[0] = nb - 1 - n;
+    m.map.excess_counter_[0] = next_offset;
+    m.writeToDisk(std::string(path));
+    printf("{\"sizeof_voxel\": %d, \"sizeof_hash_entry\": %d, \"offsetof_voxel\": [%d, %d, %d], "
+           "\"offsetof_hash_entry\": [%d, %d, %d], \"size\": [%d, %d, %d], \"blocks\": [",
+           (int)sizeof(Voxel), (int)sizeof(HashEntry), (int)offsetof(Voxel, sdf), (int)offsetof(Voxel, weight),
+           (int)offsetof(Voxel, rgb), (int)offsetof(HashEntry, ptr_), (int)offsetof(HashEntry, offset_),
+           (int)offsetof(HashEntry, pos_), nb, ne, nbk);
+    for (int b = 0; b < n; ++b) printf("%s[%d,%d,%d]", b ? "," : "", pos[b][0], pos[b][1], pos[b][2]);
+    printf("]}\n");
+    m.release();
+    return 0;
+}
+
+int main(int argc, char **argv) {
+    if (argc > 2 && std::strcmp(argv[1], "dump") == 0) return dump_pin(argv[2]);
     const int coords[] = {0, 1, -1, 7, -7, 8, -8, 9, -9, 100, -100, 4097, -4097, 65535, -65536, 1048575, -1048575,
                           2147483647, -2147483647 - 1, 123456789, -987654321};
     const int nc = sizeof(coords) / sizeof(coords[0]);

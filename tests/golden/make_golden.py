@@ -3,7 +3,8 @@
 Builds oracle/ref_pin/build_ref.sh (the reference's map_struct.cu hash and
 coordinate converters, voxel.h packing, intrinsic_matrix.h pyramid and
 device_tables.h marching-cubes tables, compiled from the reference sources
-where they lie) and records its outputs.  The marching-cubes tables are
+where they lie) and records its outputs, plus a small map dump written by the
+reference's MapStruct::writeToDisk (tests/golden/ref_dump_small.bin + .txt).  The marching-cubes tables are
 recorded as SHA-256 digests of their canonical JSON text, so the fixture pins
 them without carrying a copy.  Needs the reference tree, so it runs here, not
 on the GPU machine; the committed JSON is what the tests read.
@@ -39,6 +40,11 @@ def main() -> None:
         "triangle_table_sha256": digest(data["triangle_table"]),
         "triangle_counts": [sum(1 for v in row if v != -1) // 3 for row in data["triangle_table"]],
     }
+    # the reference's own MapStruct::writeToDisk on a small chained map (pin_main.cu dump_pin)
+    dump = ROOT / "tests/golden/ref_dump_small.bin"
+    lines = subprocess.run([exe, "dump", str(dump)], check=True, capture_output=True, text=True).stdout.splitlines()
+    out["map_dump"] = json.loads(next(l for l in lines if l.startswith("{")))
+    out["map_dump"]["file"] = dump.name
     dst = ROOT / "tests/golden/reference_pins.json"
     dst.write_text(json.dumps(out, indent=1) + "\n")
     print(f"wrote {dst}")
