@@ -102,11 +102,11 @@ __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
 }
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 
-// ToVector3i (vector_type.h:218-225): truncate, then step down when above.
-__device__ __forceinline__ int floor_ref(float v) {
-    int b = __float2int_rz(v);
-    return ((float)b > v) ? b - 1 : b;
-}
+// ToVector3i (vector_type.h:218-225): truncate, then step down when above --
+// floor(v), one round-down conversion.  The two differ only below -2^31, where
+// the reference's step down overflows; such positions are outside the map's
+// coordinate range either way.
+__device__ __forceinline__ int floor_ref(float v) { return __float2int_rd(v); }
 
 // voxelPosToBlockPos (map_struct.cu:626-636): (v < 0 ? v - 7 : v) / 8 with
 // truncating division is floor(v / 8), an arithmetic shift

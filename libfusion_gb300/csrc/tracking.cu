@@ -220,13 +220,46 @@ __device__ __forceinline__ bool rgb_row(const SessionView &sv, int level, int cs
     return true;
 }
 
+// The 28 products of the row's upper triangle added into the running sums, one
+// fused multiply-add each (the sums are a reduction compared within a
+// tolerance, not bit for bit; the rows themselves keep the reference's rounding).
 __device__ __forceinline__ void accumulate(float *acc, const float row[7]) {
     int k = 0;
 #pragma unroll
     for (int i = 0; i < 7; ++i)
 #pragma unroll
-        for (int j = i; j < 7; ++j) acc[k++] += row[i] * row[j];
+        for (int j = i; j < 7; ++j, ++k) acc[k] = __fmaf_rn(row[i], row[j], acc[k]);
     acc[28] += 1.0f;
+}
+
+// Warp sum of 29 per-lane values by recursive halving: at each of the five
+// steps a lane keeps half of its values and adds its partner's copy of them
+// (xor partner), so the warp moves 31 values per lane instead of 29 x 5.  On
+// return lane l (l < 29) holds the warp total of value l.  Fixed pattern:
+// deterministic.
+template <int N>
+__device__ __forceinline__ void halve_step(float (&v)[32], int lane) {
+    const bool upper = (lane & N) != 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        const float send = upper ? v[i] : v[i + N];
+        const float keep = upper ? v[i + N] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, N);
+    }
+}
+
+__device__ __forceinline__ float warp_sum29(const float (&acc)[29]) {
+    const int lane = threadIdx.x & 31;
+    float v[32];
+#pragma unroll
+    for (int k = 0; k < 29; ++k) v[k] = acc[k];
+    v[29] = v[30] = v[31] = 0.f;
+    halve_step<16>(v, lane);
+    halve_step<8>(v, lane);
+    halve_step<4>(v, lane);
+    halve_step<2>(v, lane);
+    halve_step<1>(v, lane);
+    return v[0];
 }
 
 constexpr int kCtaPixels = kReduceThreads * kReducePixelsPerThread;  // 1024 contiguous pixels per CTA
@@ -281,14 +314,9 @@ __device__ __forceinline__ void cta_partial(const SessionView &sv, int level, in
                                   : rgb_row(sv, level, cs, T, pc, s_v[c], s_i[c], row);
         if (ok) accumulate(acc, row);
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-        for (int k = 0; k < 29; ++k) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
+    const float total = warp_sum29(acc);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < 29; ++k) warp_sums[wid][k] = acc[k];
+    if (lane < 29) warp_sums[wid][lane] = total;
     __syncthreads();
     if (lane < 29 && (wid == 0 || wid == 4)) {
         float s = 0.f;
