@@ -293,6 +293,10 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
  * and rgb8 of the session's size) instead of its staging buffers; the pointers
  * are taken at each gbf_batch_process call (NULL, NULL restores staging). */
 GBF_API gbf_status gbf_batch_set_inputs(gbf_batch *b, int32_t slot, const uint16_t *depth_dev, const uint8_t *rgb_dev);
+/* Concurrent session groups per tick (1..4, default 2): the slots are split
+ * into contiguous groups whose frames run as parallel branches of the tick
+ * (graph branches / forked streams).  Results do not depend on it. */
+GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups);
 /* Record CUDA events at the phase boundaries of every tick (captured into the
  * graph): ingest, track, alloc+visible, integrate, z-range, march, post. */
 GBF_API gbf_status gbf_batch_set_timing(gbf_batch *b, int32_t enable);

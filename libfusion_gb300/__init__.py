@@ -310,6 +310,10 @@ class FusionBatch:
     def set_timing(self, enable: bool) -> None:
         call("gbf_batch_set_timing", self._h, 1 if enable else 0)
 
+    def set_groups(self, groups: int) -> None:
+        """Run the slots as `groups` concurrent branches of each tick (1..4)."""
+        call("gbf_batch_set_groups", self._h, int(groups))
+
     def phase_ms(self) -> dict:
         """Mean per-phase milliseconds over the ticks since set_timing(True)."""
         out = (C.c_float * 8)()

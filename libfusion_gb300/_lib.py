@@ -122,6 +122,7 @@ SIGNATURES = {
     "gbf_batch_process": (C.c_int, [_P, _P, _I32, _P]),
     "gbf_batch_set_inputs": (C.c_int, [_P, _I32, _P, _P]),
     "gbf_batch_set_timing": (C.c_int, [_P, _I32]),
+    "gbf_batch_set_groups": (C.c_int, [_P, _I32]),
     "gbf_batch_phase_ms": (C.c_int, [_P, C.POINTER(C.c_float), _I32]),
     "gbf_batch_kernels": (C.c_int, [_P, C.POINTER(_I32)]),
     "gbf_synth_default": (C.c_int, [C.POINTER(SynthParams)]),

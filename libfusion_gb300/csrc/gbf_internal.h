@@ -70,4 +70,8 @@ struct gbf_batch {
     int pending[2] = {0, 0};      // phase events recorded but not yet read
     double phase_sum[8] = {};
     long long phase_n = 0;
+    static constexpr int kMaxGroups = 4;
+    int groups = 2;                                // concurrent session groups per tick
+    cudaStream_t side[kMaxGroups - 1] = {};        // branch streams of groups 1..
+    cudaEvent_t fork = nullptr, join[kMaxGroups - 1] = {};
 };

@@ -808,6 +808,11 @@ GBF_API gbf_status gbf_batch_create(int32_t max_sessions, gbf_batch **out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev[0], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev[1], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
+    for (int g = 0; e == cudaSuccess && g < gbf_batch::kMaxGroups - 1; ++g) {
+        e = cudaStreamCreateWithFlags(&b->side[g], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         gbf_batch_destroy(b);
         return cuda_error(e, "gbf_batch_create");
@@ -836,6 +841,11 @@ GBF_API gbf_status gbf_batch_destroy(gbf_batch *b) {
     }
     if (b->d_views) cudaFree(b->d_views);
     if (b->own) cudaStreamDestroy(b->own);
+    for (int g = 0; g < gbf_batch::kMaxGroups - 1; ++g) {
+        if (b->side[g]) cudaStreamDestroy(b->side[g]);
+        if (b->join[g]) cudaEventDestroy(b->join[g]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 8; ++i)
             if (b->pev[k][i]) cudaEventDestroy(b->pev[k][i]);
@@ -881,10 +891,29 @@ static void harvest(gbf_batch *b, int k) {
     b->pending[k] = 0;
 }
 
+// One tick.  With groups > 1 (and no phase timing) the slots are split into
+// contiguous groups whose frames run as parallel branches (forked streams, or
+// parallel graph branches when captured): sessions are independent, and the
+// phases of one group (latency-bound reductions, issue-bound marching) fill
+// the SMs another group's phase leaves idle.
 static void batch_enqueue(gbf_batch *b, int k, cudaStream_t st) {
     cudaMemcpyAsync(b->d_views, b->h_views[k], sizeof(SessionView) * b->nslots, cudaMemcpyHostToDevice, st);
     IngestArgs a{0, 0, nullptr, 0, nullptr, 0};
-    enqueue_frame(b->d_views, b->nslots, b->ex, b->layouts, a, st, b->timing ? b->pev[k] : nullptr);
+    const int groups = b->timing ? 1 : std::min(b->groups, b->nslots);
+    if (groups <= 1) {
+        enqueue_frame(b->d_views, b->nslots, b->ex, b->layouts, a, st, b->timing ? b->pev[k] : nullptr);
+        return;
+    }
+    cudaEventRecord(b->fork, st);
+    for (int g = 1; g < groups; ++g) cudaStreamWaitEvent(b->side[g - 1], b->fork, 0);
+    for (int g = 0; g < groups; ++g) {
+        const int lo = b->nslots * g / groups, hi = b->nslots * (g + 1) / groups;
+        enqueue_frame(b->d_views + lo, hi - lo, b->ex, b->layouts, a, g == 0 ? st : b->side[g - 1]);
+    }
+    for (int g = 1; g < groups; ++g) {
+        cudaEventRecord(b->join[g - 1], b->side[g - 1]);
+        cudaStreamWaitEvent(st, b->join[g - 1], 0);
+    }
 }
 
 GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_t use_graph, void *stream) {
@@ -946,6 +975,16 @@ GBF_API gbf_status gbf_batch_set_inputs(gbf_batch *b, int32_t slot, const uint16
     return GBF_OK;
 }
 
+GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups) {
+    if (!b || groups < 1 || groups > gbf_batch::kMaxGroups)
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_groups: 1..4 groups");
+    for (int k = 0; k < 2; ++k)
+        if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
+    if (groups != b->groups) batch_invalidate(b);
+    b->groups = groups;
+    return GBF_OK;
+}
+
 GBF_API gbf_status gbf_batch_set_timing(gbf_batch *b, int32_t enable) {
     if (!b) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_timing: null");
     for (int k = 0; k < 2; ++k)
@@ -981,7 +1020,7 @@ GBF_API gbf_status gbf_batch_phase_ms(gbf_batch *b, float *ms, int32_t n) {
 
 GBF_API gbf_status gbf_batch_kernels(gbf_batch *b, int32_t *n) {
     if (!b || !n) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_kernels: null");
-    *n = b->nslots ? kernels_per_frame(b->ex, b->layouts) : 0;
+    *n = b->nslots ? kernels_per_frame(b->ex, b->layouts) * std::min(b->groups, b->nslots) : 0;
     return GBF_OK;
 }
 

@@ -66,7 +66,7 @@ def test_batch_session_isolation(gbf):
     pa = alone.get_camera_pose()
     ma = alone.export()
 
-    for use_graph in (False, True):
+    for use_graph, groups in ((False, 1), (True, 1), (False, 2), (True, 3)):
         a = L.System(KA, cfgA)
         b = L.System(KB, cfgB)
         b2 = L.System(KB, cfgB)
@@ -77,6 +77,7 @@ def test_batch_session_isolation(gbf):
         batch.set(0, b)
         batch.set(2, a)
         batch.set(3, b2)
+        batch.set_groups(groups)
         for i in range(5):
             for sess, (d, c, T) in ((a, frA[i]), (b, frB[i]), (b2, frB[i])):
                 sess.stage(H.cuda(d), H.cuda(c))
