@@ -293,6 +293,26 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
  * and rgb8 of the session's size) instead of its staging buffers; the pointers
  * are taken at each gbf_batch_process call (NULL, NULL restores staging). */
 GBF_API gbf_status gbf_batch_set_inputs(gbf_batch *b, int32_t slot, const uint16_t *depth_dev, const uint8_t *rgb_dev);
+/* Copy slot `slot`'s frame for the NEXT gbf_batch_process from host (or
+ * device) memory into the batch's own input buffers, on `stream`.  The buffers
+ * are double-buffered by tick parity: the copy waits on the device for the
+ * tick two submissions back (the last reader of that parity), and the next
+ * gbf_batch_process waits on the device for the copy, so frames for tick k+1
+ * can be staged on a copy stream while tick k runs.  A staged frame is used by
+ * one tick (then the slot falls back to set_inputs / the session's staging). */
+GBF_API gbf_status gbf_batch_stage(gbf_batch *b, int32_t slot, const uint16_t *depth, int64_t depth_pitch,
+                                   const uint8_t *rgb, int64_t rgb_pitch, void *stream);
+/* Per-slot outcome of a tick, copied to pinned host memory at the end of every tick. */
+typedef struct gbf_slot_result {
+    double pose[16];      /* camera -> world after the tick, row-major 4x4          */
+    int32_t tracked;      /* the tick's tracking succeeded (TrackingResult::sucess) */
+    uint32_t status;      /* GBF_FLAG_* bits                                         */
+    int64_t frame_index;  /* frames the session has processed                       */
+} gbf_slot_result;
+/* Results of the last submitted tick (back = 0) or the one before (back = 1):
+ * waits for that tick, then copies min(n, slots) records.  Reading tick k-1
+ * after submitting tick k keeps the device busy while the host reads. */
+GBF_API gbf_status gbf_batch_results(gbf_batch *b, int32_t back, gbf_slot_result *out, int32_t n);
 /* Concurrent session groups per tick (1..4, default 2): the slots are split
  * into contiguous groups whose frames run as parallel branches of the tick
  * (graph branches / forked streams).  Results do not depend on it. */

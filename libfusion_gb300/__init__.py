@@ -93,9 +93,12 @@ def _ptr(t) -> int:
 
 
 def _stream(stream) -> int:
+    """cudaStream_t handle of a torch stream, a raw handle, or the current stream (None)."""
     if stream is None:
         import torch
         return torch.cuda.current_stream().cuda_stream
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream
     return int(stream)
 
 
@@ -309,6 +312,22 @@ class FusionBatch:
 
     def set_timing(self, enable: bool) -> None:
         call("gbf_batch_set_timing", self._h, 1 if enable else 0)
+
+    def stage(self, slot: int, depth, rgb, stream=None) -> None:
+        """Copy slot's frame for the next tick (host or device tensors: depth
+        (H, W) uint16 mm, rgb (H, W, 3) uint8) into the batch's double-buffered
+        inputs on `stream`; ordered on the device against the ticks."""
+        W = depth.shape[-1]
+        call("gbf_batch_stage", self._h, int(slot), depth.data_ptr(), W * 2, rgb.data_ptr(), W * 3, _stream(stream))
+
+    def results(self, back: int = 0):
+        """Outcome of the last submitted tick (back=0) or the one before (back=1):
+        poses (n, 4, 4) camera->world, tracked (n,), status (n,), frame_index (n,)."""
+        arr = (_lib.SlotResult * self.max)()
+        call("gbf_batch_results", self._h, int(back), arr, self.max)
+        poses = np.array([list(x.pose) for x in arr]).reshape(self.max, 4, 4)
+        return (poses, np.array([x.tracked for x in arr], np.int32), np.array([x.status for x in arr], np.uint32),
+                np.array([x.frame_index for x in arr], np.int64))
 
     def set_groups(self, groups: int) -> None:
         """Run the slots as `groups` concurrent branches of each tick (1..4)."""

@@ -71,6 +71,11 @@ class MapSize(C.Structure):
     _fields_ = [("num_blocks", C.c_int32), ("num_hash_entries", C.c_int32), ("num_buckets", C.c_int32)]
 
 
+class SlotResult(C.Structure):
+    _fields_ = [("pose", C.c_double * 16), ("tracked", C.c_int32), ("status", C.c_uint32),
+                ("frame_index", C.c_int64)]
+
+
 class SynthParams(C.Structure):
     _fields_ = [("room", C.c_float * 3), ("n_spheres", C.c_int32), ("n_boxes", C.c_int32),
                 ("sphere_rmin", C.c_float), ("sphere_rmax", C.c_float), ("seed", C.c_uint64),
@@ -123,6 +128,8 @@ SIGNATURES = {
     "gbf_batch_set_inputs": (C.c_int, [_P, _I32, _P, _P]),
     "gbf_batch_set_timing": (C.c_int, [_P, _I32]),
     "gbf_batch_set_groups": (C.c_int, [_P, _I32]),
+    "gbf_batch_stage": (C.c_int, [_P, _I32, _P, _I64, _P, _I64, _P]),
+    "gbf_batch_results": (C.c_int, [_P, _I32, _P, _I32]),
     "gbf_batch_phase_ms": (C.c_int, [_P, C.POINTER(C.c_float), _I32]),
     "gbf_batch_kernels": (C.c_int, [_P, C.POINTER(_I32)]),
     "gbf_synth_default": (C.c_int, [C.POINTER(SynthParams)]),

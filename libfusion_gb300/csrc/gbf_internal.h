@@ -70,6 +70,15 @@ struct gbf_batch {
     int pending[2] = {0, 0};      // phase events recorded but not yet read
     double phase_sum[8] = {};
     long long phase_n = 0;
+    // batch-owned input buffers per tick parity and slot (gbf_batch_stage)
+    std::vector<uint16_t *> stg_depth[2];
+    std::vector<uint8_t *> stg_rgb[2];
+    std::vector<size_t> stg_pixels[2];
+    std::vector<char> staged[2];                    // slot staged for the tick of this parity
+    std::vector<cudaEvent_t> staged_ev[2];          // end of the slot's staging copy
+    gbf_slot_result *d_res[2] = {nullptr, nullptr}; // per-slot results of the tick (device)
+    gbf_slot_result *h_res[2] = {nullptr, nullptr}; // pinned copies
+    long long submitted = 0;                        // ticks submitted
     static constexpr int kMaxGroups = 4;
     int groups = 2;                                // concurrent session groups per tick
     cudaStream_t side[kMaxGroups - 1] = {};        // branch streams of groups 1..

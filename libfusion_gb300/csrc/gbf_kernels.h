@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/gbfusion.h"
 #include "gbf_types.h"
 
 namespace gbf {
@@ -59,6 +60,8 @@ void launch_reduce_once(const SessionView *d_sv, const Extent &ex, int level, co
                         cudaStream_t st);
 // frame bookkeeping after tracking: pose update, reference swap
 void launch_frame_finish(const SessionView *d_sv, int nslots, cudaStream_t st);
+// per-slot pose / tracking / status record of a batch tick (empty slots zero)
+void launch_slot_results(const SessionView *d_sv, int nslots, gbf_slot_result *out, cudaStream_t st);
 
 // ---- meshing (mesh.cu) ------------------------------------------------------------
 // returns via device counters; the host reads C_MESH_TRIS

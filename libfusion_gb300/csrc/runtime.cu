@@ -813,6 +813,16 @@ GBF_API gbf_status gbf_batch_create(int32_t max_sessions, gbf_batch **out) {
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (int k = 0; k < 2; ++k) {
+        b->stg_depth[k].assign(max_sessions, nullptr);
+        b->stg_rgb[k].assign(max_sessions, nullptr);
+        b->stg_pixels[k].assign(max_sessions, 0);
+        b->staged[k].assign(max_sessions, 0);
+        b->staged_ev[k].assign(max_sessions, nullptr);
+        if (e == cudaSuccess) e = cudaMalloc(&b->d_res[k], sizeof(gbf_slot_result) * max_sessions);
+        if (e == cudaSuccess) e = cudaMallocHost(&b->h_res[k], sizeof(gbf_slot_result) * max_sessions);
+        if (e == cudaSuccess) memset(b->h_res[k], 0, sizeof(gbf_slot_result) * max_sessions);
+    }
     if (e != cudaSuccess) {
         gbf_batch_destroy(b);
         return cuda_error(e, "gbf_batch_create");
@@ -846,6 +856,15 @@ GBF_API gbf_status gbf_batch_destroy(gbf_batch *b) {
         if (b->join[g]) cudaEventDestroy(b->join[g]);
     }
     if (b->fork) cudaEventDestroy(b->fork);
+    for (int k = 0; k < 2; ++k) {
+        for (size_t i = 0; i < b->stg_depth[k].size(); ++i) {
+            if (b->stg_depth[k][i]) cudaFree(b->stg_depth[k][i]);
+            if (b->stg_rgb[k][i]) cudaFree(b->stg_rgb[k][i]);
+            if (b->staged_ev[k][i]) cudaEventDestroy(b->staged_ev[k][i]);
+        }
+        if (b->d_res[k]) cudaFree(b->d_res[k]);
+        if (b->h_res[k]) cudaFreeHost(b->h_res[k]);
+    }
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 8; ++i)
             if (b->pev[k][i]) cudaEventDestroy(b->pev[k][i]);
@@ -859,6 +878,7 @@ GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
     for (int k = 0; k < 2; ++k)
         if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
     b->sessions[slot] = s;
+    b->staged[0][slot] = b->staged[1][slot] = 0;
     batch_invalidate(b);
     b->nslots = 0;
     Extent ex;
@@ -896,12 +916,18 @@ static void harvest(gbf_batch *b, int k) {
 // parallel graph branches when captured): sessions are independent, and the
 // phases of one group (latency-bound reductions, issue-bound marching) fill
 // the SMs another group's phase leaves idle.
+static void batch_results(gbf_batch *b, int k, cudaStream_t st) {
+    launch_slot_results(b->d_views, b->nslots, b->d_res[k], st);
+    cudaMemcpyAsync(b->h_res[k], b->d_res[k], sizeof(gbf_slot_result) * b->nslots, cudaMemcpyDeviceToHost, st);
+}
+
 static void batch_enqueue(gbf_batch *b, int k, cudaStream_t st) {
     cudaMemcpyAsync(b->d_views, b->h_views[k], sizeof(SessionView) * b->nslots, cudaMemcpyHostToDevice, st);
     IngestArgs a{0, 0, nullptr, 0, nullptr, 0};
     const int groups = b->timing ? 1 : std::min(b->groups, b->nslots);
     if (groups <= 1) {
         enqueue_frame(b->d_views, b->nslots, b->ex, b->layouts, a, st, b->timing ? b->pev[k] : nullptr);
+        batch_results(b, k, st);
         return;
     }
     cudaEventRecord(b->fork, st);
@@ -914,6 +940,7 @@ static void batch_enqueue(gbf_batch *b, int k, cudaStream_t st) {
         cudaEventRecord(b->join[g - 1], b->side[g - 1]);
         cudaStreamWaitEvent(st, b->join[g - 1], 0);
     }
+    batch_results(b, k, st);
 }
 
 GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_t use_graph, void *stream) {
@@ -934,7 +961,13 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
         if (b->sessions[i]) {
             hv[i] = b->sessions[i]->view;
             hv[i].active = active[i] ? 1 : 0;
-            if (b->in_depth[i]) {
+            if (b->staged[k][i]) {
+                hv[i].in_depth = b->stg_depth[k][i];
+                hv[i].in_rgb = b->stg_rgb[k][i];
+                cudaError_t e = cudaStreamWaitEvent(st, b->staged_ev[k][i], 0);
+                if (e != cudaSuccess) return cuda_error(e, "gbf_batch_process: wait for staging");
+                b->staged[k][i] = 0;
+            } else if (b->in_depth[i]) {
                 hv[i].in_depth = b->in_depth[i];
                 hv[i].in_rgb = b->in_rgb[i];
             }
@@ -964,7 +997,60 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
     b->ev_used[k] = true;
     b->pending[k] = b->timing;
     b->last = k;
+    b->submitted += 1;
     return check_cuda("gbf_batch_process");
+}
+
+GBF_API gbf_status gbf_batch_stage(gbf_batch *b, int32_t slot, const uint16_t *depth, int64_t depth_pitch,
+                                   const uint8_t *rgb, int64_t rgb_pitch, void *stream) {
+    if (!b || slot < 0 || slot >= b->max_slots || !depth || !rgb)
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_stage: bad slot or pointers");
+    gbf_session *s = b->sessions[slot];
+    if (!s) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_stage: empty slot");
+    const int W = s->K.width, H = s->K.height;
+    if (depth_pitch < W * 2 || rgb_pitch < W * 3)
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_stage: pitch smaller than a row");
+    const int k = b->flip;  // parity of the next tick
+    cudaError_t e = cudaSuccess;
+    const size_t px = (size_t)W * H;
+    if (b->stg_pixels[k][slot] != px) {  // first use of the slot, or a session of another size
+        if (b->ev_used[k]) e = cudaEventSynchronize(b->ev[k]);
+        if (b->stg_depth[k][slot]) cudaFree(b->stg_depth[k][slot]);
+        if (b->stg_rgb[k][slot]) cudaFree(b->stg_rgb[k][slot]);
+        b->stg_depth[k][slot] = nullptr;
+        b->stg_rgb[k][slot] = nullptr;
+        b->stg_pixels[k][slot] = 0;
+        if (e == cudaSuccess) e = cudaMalloc(&b->stg_depth[k][slot], px * 2);
+        if (e == cudaSuccess) e = cudaMalloc(&b->stg_rgb[k][slot], px * 3);
+        if (e == cudaSuccess && !b->staged_ev[k][slot])
+            e = cudaEventCreateWithFlags(&b->staged_ev[k][slot], cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_error(e, "gbf_batch_stage: buffers");
+        b->stg_pixels[k][slot] = px;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    // the tick two submissions back read these buffers
+    if (b->ev_used[k]) e = cudaStreamWaitEvent(st, b->ev[k], 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(b->stg_depth[k][slot], (size_t)W * 2, depth, depth_pitch, (size_t)W * 2, H,
+                              cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(b->stg_rgb[k][slot], (size_t)W * 3, rgb, rgb_pitch, (size_t)W * 3, H,
+                              cudaMemcpyDefault, st);
+    if (e == cudaSuccess) e = cudaEventRecord(b->staged_ev[k][slot], st);
+    if (e != cudaSuccess) return cuda_error(e, "gbf_batch_stage");
+    b->staged[k][slot] = 1;
+    return GBF_OK;
+}
+
+GBF_API gbf_status gbf_batch_results(gbf_batch *b, int32_t back, gbf_slot_result *out, int32_t n) {
+    if (!b || !out || n < 0 || back < 0 || back > 1)
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_results: bad arguments");
+    if (b->submitted <= back) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_results: no such tick");
+    const int k = back == 0 ? b->last : (b->last ^ 1);
+    cudaError_t e = cudaEventSynchronize(b->ev[k]);
+    if (e != cudaSuccess) return cuda_error(e, "gbf_batch_results");
+    memcpy(out, b->h_res[k], sizeof(gbf_slot_result) * std::min(n, b->nslots));
+    return GBF_OK;
 }
 
 GBF_API gbf_status gbf_batch_set_inputs(gbf_batch *b, int32_t slot, const uint16_t *depth_dev, const uint8_t *rgb_dev) {
@@ -1020,7 +1106,7 @@ GBF_API gbf_status gbf_batch_phase_ms(gbf_batch *b, float *ms, int32_t n) {
 
 GBF_API gbf_status gbf_batch_kernels(gbf_batch *b, int32_t *n) {
     if (!b || !n) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_kernels: null");
-    *n = b->nslots ? kernels_per_frame(b->ex, b->layouts) * std::min(b->groups, b->nslots) : 0;
+    *n = b->nslots ? kernels_per_frame(b->ex, b->layouts) * std::min(b->groups, b->nslots) + 1 : 0;
     return GBF_OK;
 }
 

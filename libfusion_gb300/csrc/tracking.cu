@@ -578,6 +578,34 @@ void launch_frame_finish(const SessionView *d_sv, int nslots, cudaStream_t st) {
     track_finish_kernel<<<nslots, 32, 0, st>>>(d_sv, 1);
 }
 
+namespace {
+__global__ void slot_results_kernel(const SessionView *svs, int n, gbf_slot_result *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SessionView &sv = svs[i];
+    gbf_slot_result r;
+    if (!sv.ts) {  // empty slot
+        for (int j = 0; j < 16; ++j) r.pose[j] = 0.0;
+        r.tracked = 0;
+        r.status = 0u;
+        r.frame_index = 0;
+    } else {
+        const TrackState *ts = sv.ts;
+        for (int j = 0; j < 12; ++j) r.pose[j] = ts->pose[j];
+        r.pose[12] = r.pose[13] = r.pose[14] = 0.0;
+        r.pose[15] = 1.0;
+        r.tracked = ts->success;
+        r.status = (uint32_t)sv.ctr[C_STATUS];
+        r.frame_index = ts->frame_index;
+    }
+    out[i] = r;
+}
+}  // namespace
+
+void launch_slot_results(const SessionView *d_sv, int nslots, gbf_slot_result *out, cudaStream_t st) {
+    slot_results_kernel<<<(nslots + 127) / 128, 128, 0, st>>>(d_sv, nslots, out);
+}
+
 }  // namespace gbf
 
 // ============================================================================

@@ -70,7 +70,7 @@ typedef struct or_system_f64 or_system_f64;
     /* DenseMapping::raycast: z-range tiles of the last fuse's visible blocks + march; vmap float4 */              \
     int or_raycast_##S(or_map_##S *m, const double T[16], float *vmap);                                            \
     int64_t or_map_blocks_##S(const or_map_##S *m);                                                                \
-    void or_ray_stats_##S(or_map_##S *m, const double T[16], long long out[5], int32_t *steps_per_pixel);            \
+    void or_ray_stats_##S(or_map_##S *m, const double T[16], long long out[7], int32_t *steps_per_pixel);            \
     int64_t or_map_export_##S(const or_map_##S *m, int32_t *coords, float *sdf, float *w, uint8_t *rgb,           \
                               int64_t max_blocks);                                                                 \
     int64_t or_visible_##S(const or_map_##S *m, int32_t *coords, int64_t max_blocks);                              \

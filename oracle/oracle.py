@@ -161,12 +161,14 @@ class OracleMap:
 
     def ray_stats(self, pose, per_pixel: bool = False):
         """March counts of a raycast at `pose` (rays, steps, voxel samples,
-        trilinear reads, hits); with per_pixel, also each pixel's cost in
-        samples (steps + 8 per trilinear read)."""
-        out = (C.c_longlong * 5)()
+        trilinear reads, hits, steps through unallocated or unobserved space,
+        nearest reads in unallocated blocks);
+        with per_pixel, also each pixel's cost in samples (steps + 8 per
+        trilinear read)."""
+        out = (C.c_longlong * 7)()
         pp = np.zeros((self.K.height, self.K.width), np.int32) if per_pixel else None
         self.fn("or_ray_stats")(self.h, _d16(pose), out, _p(pp))
-        d = dict(zip(("rays", "steps", "samples", "interps", "hits"), out[:]))
+        d = dict(zip(("rays", "steps", "samples", "interps", "hits", "empty", "missing"), out[:]))
         return (d, pp) if per_pixel else d
 
     def export(self):

@@ -482,7 +482,7 @@ static void zrange_pass(MAP *m, const M34 *Tcw) {
 }
 
 /* march statistics for the raycast roofline: samples, trilinear reads, steps, rays */
-typedef struct { long long samples, interps, steps, rays, hits; } RayStats;
+typedef struct { long long samples, interps, steps, rays, hits, empty, missing; } RayStats;
 static _Thread_local RayStats *g_rs;
 
 /* read_sdf (ray_tracing.cu:291-305) */
@@ -490,6 +490,7 @@ static R read_sdf(const MAP *m, R px, R py, R pz, int *valid) {
     if (g_rs) g_rs->samples++;
     const int vx = floor_r(px), vy = floor_r(py), vz = floor_r(pz);
     const int id = map_find(m, vtob(vx), vtob(vy), vtob(vz));
+    if (id < 0 && g_rs) g_rs->missing++;
     if (id >= 0) {
         const size_t i = (size_t)id * 512 + vtol(vz) * 64 + vtol(vy) * 8 + vtol(vx);
         if (vox_w(m, i) != 0) {
@@ -559,6 +560,7 @@ static void ray_pixel(const MAP *m, const M34 *Twc, const M34 *Tcw, int x, int y
         if (sdf <= 0) break;
         if (sdf >= 0 && last_sdf < 0) return;
         step = valid ? RFMAX(sdf * m->step_scale, (R)1) : (R)2;
+        if (g_rs && !valid) g_rs->empty++;
         r = v3(r.x + dir.x * step, r.y + dir.y * step, r.z + dir.z * step);
         dist_s += step;
     }
@@ -597,12 +599,12 @@ int SFX(or_raycast)(MAP *m, const double T[16], float *vmap) {
 /* counts of the last fuse's raycast at pose T (single thread): rays marched,
  * march steps, voxel samples (each a hash lookup + one voxel read), trilinear
  * reads, hits */
-void SFX(or_ray_stats)(MAP *m, const double T[16], long long out[5], int32_t *steps_per_pixel) {
+void SFX(or_ray_stats)(MAP *m, const double T[16], long long out[7], int32_t *steps_per_pixel) {
     double inv[12];
     pose_inv(T, inv);
     const M34 Twc = to_m(T), Tcw = to_m(inv);
     zrange_pass(m, &Tcw);
-    RayStats rs = {0, 0, 0, 0, 0};
+    RayStats rs = {0, 0, 0, 0, 0, 0, 0};
     g_rs = &rs;
     float px[4];
     if (m->nvis && m->nrender)
@@ -614,6 +616,7 @@ void SFX(or_ray_stats)(MAP *m, const double T[16], long long out[5], int32_t *st
             }
     g_rs = NULL;
     out[0] = rs.rays; out[1] = rs.steps; out[2] = rs.samples; out[3] = rs.interps; out[4] = rs.hits;
+    out[5] = rs.empty; out[6] = rs.missing;
 }
 
 int64_t SFX(or_map_blocks)(const MAP *m) { return m->n_used; }
