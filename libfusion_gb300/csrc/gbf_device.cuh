@@ -192,6 +192,30 @@ __device__ __forceinline__ float unpack_sw(unsigned lo, unsigned hi, float &w) {
     }
 }
 
+// load_vox / store_sw on explicit pool pointers (no descriptor reads)
+template <int LAYOUT>
+__device__ __forceinline__ Vox load_vox_at(const void *__restrict__ sw, const uchar4 *__restrict__ rgb, int i) {
+    Vox v;
+    if (LAYOUT == GBF_VOXEL_REF) {
+        const uint2 q = reinterpret_cast<const uint2 *>(sw)[i];
+        v.sdf = unpack_sw<LAYOUT>(q.x, q.y, v.w);
+    } else {
+        const unsigned q = reinterpret_cast<const unsigned *>(sw)[i];
+        v.sdf = unpack_sw<LAYOUT>(q, 0u, v.w);
+    }
+    v.rgb = rgb[i];
+    return v;
+}
+template <int LAYOUT>
+__device__ __forceinline__ void store_sw_at(void *__restrict__ sw, int i, float sdf, float w) {
+    if (LAYOUT == GBF_VOXEL_REF)
+        reinterpret_cast<uint2 *>(sw)[i] =
+            make_uint2((unsigned)(unsigned short)sdf_ref_pack(sdf), __float_as_uint(weight_ref_store(w)));
+    else
+        reinterpret_cast<unsigned *>(sw)[i] =
+            (unsigned)__half_as_ushort(__float2half_rn(sdf)) | ((unsigned)weight_half_pack(w) << 16);
+}
+
 template <int LAYOUT>
 __device__ __forceinline__ Vox load_vox(const SessionView &sv, size_t i) {
     Vox v;

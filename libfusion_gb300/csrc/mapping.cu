@@ -216,31 +216,42 @@ __global__ void visible_kernel(const SessionView *svs) {
     }
 }
 
-constexpr int kIntThreads = 128;  // threads per integration CTA (512 / kIntThreads voxels each)
+constexpr int kIntThreads = 128;  // threads per integration CTA (512 / kIntThreads voxels each), 12 CTAs per SM
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(kIntThreads) integrate_kernel(const SessionView *svs, int mode) {
+__global__ void __launch_bounds__(kIntThreads, 12) integrate_kernel(const SessionView *svs, int mode) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || sv.layout != LAYOUT) return;
-    __shared__ M34 Tcw;
-    if (threadIdx.x == 0) Tcw = load_m34(sv.ts->map_tcw);
+    __shared__ M34 Tcw_s;
+    if (threadIdx.x == 0) Tcw_s = load_m34(sv.ts->map_tcw);
     __syncthreads();
-    const LevelK &K = sv.lv[0];
+    // Everything the voxel loop reads from the session descriptor is copied to
+    // registers first: the loop stores voxels through global pointers, which the
+    // compiler would otherwise have to assume may alias the descriptor.
+    const M34 Tcw = Tcw_s;
+    const LevelK K = sv.lv[0];
     const int W = K.w, H = K.h;
     const int nvis = sv.ctr[C_NVIS];
     if (blockIdx.x == 0 && threadIdx.x == 0) sv.ts->integrated_blocks += nvis;
     const float voxel = sv.voxel, tau = sv.tau, inv_tau = sv.inv_tau;
+    const int *__restrict__ vis = sv.vis;
+    const int4 *__restrict__ bcoord = sv.bcoord;
+    const float2 *__restrict__ fuse_px = sv.fuse_px;
+    const uchar4 *__restrict__ rgb4 = sv.rgb4;
+    unsigned char *__restrict__ bfresh = sv.bfresh;
+    void *__restrict__ vox_sw = sv.vox_sw;
+    uchar4 *__restrict__ vox_rgb = sv.vox_rgb;
 
     for (int b = blockIdx.x; b < nvis; b += gridDim.x) {
-        const int tagged = sv.vis[b];
+        const int tagged = vis[b];
         const int id = tagged & 0x7fffffff;
         const bool fresh = tagged < 0;
-        const int4 bc = sv.bcoord[id];
+        const int4 bc = bcoord[id];
 #pragma unroll
         for (int half_i = 0; half_i < kBlockVoxels / kIntThreads; ++half_i) {
             const int li = threadIdx.x + half_i * kIntThreads;
             const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
-            const size_t vi = (size_t)id * kBlockVoxels + li;
+            const int vi = id * kBlockVoxels + li;
             const float3 p = Tcw.apply((float)(bc.x * 8 + lx) * voxel, (float)(bc.y * 8 + ly) * voxel,
                                        (float)(bc.z * 8 + lz) * voxel);
             const int u = __float2int_rd(((K.fx * p.x) / p.z + K.cx) + 0.5f);
@@ -249,7 +260,7 @@ __global__ void __launch_bounds__(kIntThreads) integrate_kernel(const SessionVie
             float dist = 0.f, weight = 0.f, sdf = 0.f;
             if (upd) {
                 // depth and weight of the pixel, rejected pixels as NaN (fuse_px)
-                const float2 fp = sv.fuse_px[(size_t)v * W + u];
+                const float2 fp = fuse_px[v * W + u];
                 dist = fp.x;
                 weight = fp.y;
                 upd = !isnan(dist);
@@ -260,8 +271,8 @@ __global__ void __launch_bounds__(kIntThreads) integrate_kernel(const SessionVie
             }
             if (!upd) {
                 if (fresh) {
-                    store_sw<LAYOUT>(sv, vi, 0.f, 0.f);
-                    sv.vox_rgb[vi] = make_uchar4(0, 0, 0, 0);
+                    store_sw_at<LAYOUT>(vox_sw, vi, 0.f, 0.f);
+                    vox_rgb[vi] = make_uchar4(0, 0, 0, 0);
                 }
                 continue;
             }
@@ -270,9 +281,9 @@ __global__ void __launch_bounds__(kIntThreads) integrate_kernel(const SessionVie
             if (fresh) {
                 old.sdf = 0.f; old.w = 0.f; old.rgb = make_uchar4(0, 0, 0, 0);
             } else {
-                old = load_vox<LAYOUT>(sv, vi);
+                old = load_vox_at<LAYOUT>(vox_sw, vox_rgb, vi);
             }
-            const uchar4 cn = sv.rgb4[(size_t)v * W + u];
+            const uchar4 cn = rgb4[v * W + u];
             float nsdf, nw;
             uchar4 nrgb;
             if (old.w == 0.f) {
@@ -286,10 +297,10 @@ __global__ void __launch_bounds__(kIntThreads) integrate_kernel(const SessionVie
                 nrgb.z = (unsigned char)__float2int_rz(((float)old.rgb.z * old.w + (float)cn.z * weight) / den);
                 nrgb.w = 0;
             }
-            store_sw<LAYOUT>(sv, vi, nsdf, nw);
-            sv.vox_rgb[vi] = nrgb;
+            store_sw_at<LAYOUT>(vox_sw, vi, nsdf, nw);
+            vox_rgb[vi] = nrgb;
         }
-        if (fresh && threadIdx.x == 0) sv.bfresh[id] = 0;
+        if (fresh && threadIdx.x == 0) bfresh[id] = 0;
     }
 }
 
