@@ -18,6 +18,8 @@
  *   DenseMapping::update(frame)            src/voxel_hashing/voxel_hashing.cpp:44-65  -> gbf_fuse (nmap given)
  *   DenseMapping::update(depth,image,pose) src/voxel_hashing/voxel_hashing.cpp:67-85  -> gbf_fuse (nmap NULL)
  *   DenseMapping::raycast                  src/voxel_hashing/voxel_hashing.cpp:87-119 -> gbf_raycast
+ *   DenseMapping::raycast_check_visibility src/voxel_hashing/voxel_hashing.cpp:121-135 -> gbf_raycast_check_visibility
+ *   renderScene / renderSceneTextured      src/tracking/cuda_imgproc.cu:50-108        -> gbf_render_scene, gbf_session_render
  *   DenseMapping::reset_mapping            src/voxel_hashing/voxel_hashing.cpp:137-140 -> gbf_session_reset
  *   DenseMapping::fetch_mesh_*             src/voxel_hashing/voxel_hashing.cpp:142-187 -> gbf_extract_mesh
  *   DenseMapping::write/readMapFromDisk    src/voxel_hashing/voxel_hashing.cpp:189-205 -> gbf_map_write_dump / gbf_map_read_dump
@@ -170,6 +172,26 @@ GBF_API gbf_status gbf_fuse(gbf_session *s, const float *depth_dev, int64_t dept
  * untouched when the last fuse saw no visible / renderable block. */
 GBF_API gbf_status gbf_raycast(gbf_session *s, const double T_wc[16],
                                float *vmap_dev, int64_t vmap_pitch, void *stream);
+/* DenseMapping::raycast_check_visibility (src/voxel_hashing/voxel_hashing.cpp:121-135):
+ * the visible-block list recomputed for pose T by the frustum test alone
+ * (count_visible_entry, src/voxel_hashing/ray_tracing.cu:778-807) over every
+ * allocated block, then gbf_raycast at T -- a raycast from any pose, e.g. for
+ * relocalisation.  The list replaces the last fuse's, as in the reference. */
+GBF_API gbf_status gbf_raycast_check_visibility(gbf_session *s, const double T[16], float *vmap, int64_t vmap_pitch,
+                                                void *stream);
+/* renderScene / renderSceneTextured (src/tracking/cuda_imgproc.cu:50-108): Phong
+ * shading of a camera-frame vertex and normal map (float4, pitched) into RGBA8,
+ * light at (5, 5, 5) in the camera frame; rgb8 (pitched) textures it, NULL =
+ * white.  Device pointers. */
+GBF_API gbf_status gbf_render_scene(const float *vmap, int64_t vmap_pitch, const float *nmap, int64_t nmap_pitch,
+                                    const uint8_t *rgb, int64_t rgb_pitch, int32_t width, int32_t height,
+                                    uint8_t *out, int64_t out_pitch, void *stream);
+/* DeviceImage::get_rendered_image / get_rendered_scene_textured
+ * (src/tracking/device_image.cpp:119-129): the session's model prediction (the
+ * level-0 vertex and normal maps of its last raycast) shaded; textured with the
+ * last fused frame's colour. */
+GBF_API gbf_status gbf_session_render(gbf_session *s, int32_t textured, uint8_t *out, int64_t out_pitch,
+                                      void *stream);
 /* Marching cubes over all allocated blocks into caller-allocated device
  * buffers (3 float3 per triangle; attr: 3 float3 normals or 3 uchar3 colours).
  * *n_tris receives the triangle count clamped to max_tris (synchronises). */
@@ -275,6 +297,21 @@ GBF_API gbf_status gbf_map_write_dump(gbf_session *s, const char *path, const gb
  * are kept, as in the reference, which uploads only the map storage.
  * Synchronises. */
 GBF_API gbf_status gbf_map_read_dump(gbf_session *s, const char *path);
+
+/* ---- block garbage collection ------------------------------------------------- */
+/* deleteBlock (src/data_struct/map_struct.cu:327-363) for a list of blocks: their
+ * voxels and table entries go, the pool is compacted.  The reference defines
+ * deleteBlock but never calls it (its one caller is commented out,
+ * depth_fusion.cu:70), so its pool only grows; a long-running session prunes
+ * here.  A deleted block that is observed again starts from zero, as a block
+ * the reference re-creates would.  Pose and tracking state are kept.
+ * Synchronises; *n_deleted (may be NULL) = blocks removed. */
+GBF_API gbf_status gbf_map_delete_blocks(gbf_session *s, const int32_t *coords, int64_t n, int64_t *n_deleted);
+/* Delete the blocks whose centre lies farther than `radius` metres from
+ * `center` (world frame; center NULL or radius < 0: no distance test) and, with
+ * drop_unobserved, the blocks without any observed voxel (all weights 0). */
+GBF_API gbf_status gbf_map_prune(gbf_session *s, const double center[3], double radius, int32_t drop_unobserved,
+                                 int64_t *n_deleted);
 
 /* Visible-block list of the last fuse (block coordinates), synchronises. */
 GBF_API gbf_status gbf_visible_blocks(gbf_session *s, int32_t *coords, int64_t max_blocks, int64_t *n_blocks);

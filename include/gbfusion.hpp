@@ -128,6 +128,10 @@ class DenseMapping : public Session {
               "fetch_mesh_with_colour");
         return (size_t)n;
     }
+    void raycast_check_visibility(DeviceImageView &vmap, const Pose &pose, void *stream = nullptr) {
+        check(gbf_raycast_check_visibility(handle(), pose.data(), (float *)vmap.data, vmap.pitch, stream),
+              "raycast_check_visibility");
+    }
     // the reference's raw dump: file_name + file_name.txt (reference default sizes)
     void writeMapToDisk(const std::string &file_name) {
         check(gbf_map_write_dump(handle(), file_name.c_str(), nullptr), "writeMapToDisk");

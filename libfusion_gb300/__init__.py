@@ -27,7 +27,7 @@ from ._lib import (FLAG_COORD_RANGE, FLAG_HASH_FULL, FLAG_NAN_POSE, FLAG_POOL_EX
 
 __all__ = [
     "IntrinsicMatrix", "DenseMapping", "DenseTracking", "System", "FusionBatch", "SynthScene", "TrackingResult",
-    "write_dump", "read_dump",
+    "write_dump", "read_dump", "render_scene",
     "default_config", "session_bytes", "GbfError", "VOXEL_REF", "VOXEL_HALF", "MESH_VERTEX", "MESH_NORMAL",
     "MESH_COLOUR", "FLAG_POOL_EXHAUSTED", "FLAG_HASH_FULL", "FLAG_COORD_RANGE", "FLAG_TRACK_FAILED",
     "FLAG_NAN_POSE", "version",
@@ -168,6 +168,11 @@ class DenseMapping(_Session):
     def raycast(self, vmap, pose, stream=None) -> None:
         call("gbf_raycast", self._h, mat16(pose), _ptr(vmap), self.K.width * 16, _stream(stream))
 
+    def raycast_check_visibility(self, vmap, pose, stream=None) -> None:
+        """Visible blocks recomputed for `pose` (frustum test over every allocated
+        block), then raycast at `pose` into `vmap`."""
+        call("gbf_raycast_check_visibility", self._h, mat16(pose), _ptr(vmap), self.K.width * 16, _stream(stream))
+
     def reset_mapping(self, stream=None) -> None:
         self.reset(stream)
 
@@ -221,6 +226,21 @@ class DenseMapping(_Session):
         """DenseMapping::readMapFromDisk (src/voxel_hashing/voxel_hashing.cpp:198-205):
         replaces the map with the dump's blocks; pose and tracking state stay."""
         call("gbf_map_read_dump", self._h, str(file_name).encode())
+
+    def delete_blocks(self, coords) -> int:
+        """Remove the listed blocks (block coordinates); returns how many were removed."""
+        c = np.ascontiguousarray(coords, np.int32).reshape(-1, 3)
+        n = C.c_int64()
+        call("gbf_map_delete_blocks", self._h, c.ctypes.data if len(c) else None, len(c), C.byref(n))
+        return int(n.value)
+
+    def prune(self, center=None, radius: float = -1.0, drop_unobserved: bool = False) -> int:
+        """Remove blocks farther than `radius` m from `center` and/or without any
+        observed voxel; returns how many were removed."""
+        n = C.c_int64()
+        ctr = None if center is None else (C.c_double * 3)(*[float(x) for x in center])
+        call("gbf_map_prune", self._h, ctr, float(radius), 1 if drop_unobserved else 0, C.byref(n))
+        return int(n.value)
 
     def visible_blocks(self) -> np.ndarray:
         n = C.c_int64()
@@ -285,6 +305,20 @@ class System(DenseTracking):
 
     def get_camera_pose(self, stream=None) -> np.ndarray:
         return self.get_pose(stream)
+
+    def _render(self, textured: bool, stream=None):
+        import torch
+        out = torch.empty((self.K.height, self.K.width, 4), dtype=torch.uint8, device="cuda")
+        call("gbf_session_render", self._h, 1 if textured else 0, out.data_ptr(), self.K.width * 4, _stream(stream))
+        return out
+
+    def get_rendered_image(self, stream=None):
+        """Phong-shaded model prediction, (H, W, 4) uint8 on the device."""
+        return self._render(False, stream)
+
+    def get_rendered_scene_textured(self, stream=None):
+        """The same shading with the last frame's colour."""
+        return self._render(True, stream)
 
 
 class FusionBatch:
@@ -356,6 +390,17 @@ class FusionBatch:
             self.close()
         except Exception:
             pass
+
+
+def render_scene(vmap, nmap, rgb=None, stream=None):
+    """renderScene / renderSceneTextured: (H, W, 4) float32 camera-frame vertex and
+    normal maps (CUDA tensors), optional (H, W, 3) uint8 colour -> (H, W, 4) uint8."""
+    import torch
+    h, w = vmap.shape[:2]
+    out = torch.empty((h, w, 4), dtype=torch.uint8, device=vmap.device)
+    call("gbf_render_scene", _ptr(vmap), w * 16, _ptr(nmap), w * 16, None if rgb is None else _ptr(rgb), w * 3,
+         w, h, out.data_ptr(), w * 4, _stream(stream))
+    return out
 
 
 def write_dump(file_name: str, coords, sdf, weight, rgb, size: tuple[int, int, int] | None = None) -> None:

@@ -115,9 +115,14 @@ SIGNATURES = {
     "gbf_process_frame_staged": (C.c_int, [_P, _P]),
     "gbf_map_export": (C.c_int, [_P, _P, _P, _P, _P, _I64, C.POINTER(C.c_int64)]),
     "gbf_map_import": (C.c_int, [_P, _P, _P, _P, _P, _I64]),
+    "gbf_raycast_check_visibility": (C.c_int, [_P, _D16, _P, _I64, _P]),
+    "gbf_render_scene": (C.c_int, [_P, _I64, _P, _I64, _P, _I64, _I32, _I32, _P, _I64, _P]),
+    "gbf_session_render": (C.c_int, [_P, _I32, _P, _I64, _P]),
     "gbf_dump_write": (C.c_int, [C.c_char_p, _P, _P, _P, _P, _P, _I64]),
     "gbf_dump_read": (C.c_int, [C.c_char_p, _P, _P, _P, _P, _P, _I64, C.POINTER(C.c_int64)]),
     "gbf_map_write_dump": (C.c_int, [_P, C.c_char_p, _P]),
+    "gbf_map_delete_blocks": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_int64)]),
+    "gbf_map_prune": (C.c_int, [_P, _P, C.c_double, _I32, C.POINTER(C.c_int64)]),
     "gbf_map_read_dump": (C.c_int, [_P, C.c_char_p]),
     "gbf_visible_blocks": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_int64)]),
     "gbf_zrange": (C.c_int, [_P, _P, _I64]),

@@ -41,6 +41,12 @@ void launch_fuse_import(const SessionView *d_sv, const Extent &ex, const FuseImp
 void launch_fuse(const SessionView *d_sv, int nslots, const Extent &ex, int mode, const int *layouts,
                  cudaStream_t st);
 void launch_alloc_visible(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st);
+// visible list = allocated blocks in the frustum of the map pose (no fuse)
+void launch_visible_frustum(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st);
+// Phong shading of camera-frame vertex / normal maps into RGBA8 (rgb NULL = untextured)
+void launch_render(const float4 *vmap, long long vmap_pitch, const float4 *nmap, long long nmap_pitch,
+                   const uint8_t *rgb, long long rgb_pitch, int rgb_stride, int w, int h, uchar4 *out,
+                   long long out_pitch, cudaStream_t st);
 void launch_integrate(const SessionView *d_sv, int nslots, const Extent &ex, int mode, const int *layouts,
                       cudaStream_t st);
 

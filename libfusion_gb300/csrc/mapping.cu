@@ -192,6 +192,16 @@ __device__ __forceinline__ bool block_in_frustum(const SessionView &sv, const M3
     return false;
 }
 
+__global__ void vis_begin_kernel(const SessionView *svs) {
+    const SessionView &sv = svs[blockIdx.x];
+    if (!sv.active || threadIdx.x != 0) return;
+    sv.ctr[C_NVIS] = 0;
+}
+
+// touched: also count blocks stamped by this fuse (check_visibility_flag_kernel's
+// flag 2); without it, the frustum test alone (count_visible_entry,
+// ray_tracing.cu:778-807 with VisibleEntryEvaluateFunctor, :681-710).
+template <bool TOUCHED>
 __global__ void visible_kernel(const SessionView *svs) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
@@ -208,7 +218,7 @@ __global__ void visible_kernel(const SessionView *svs) {
         int tag = 0;
         if (id < n) {
             const int4 c = sv.bcoord[id];
-            vis = (sv.bstamp[id] == frame) || block_in_frustum(sv, Tcw, c.x, c.y, c.z);
+            vis = (TOUCHED && sv.bstamp[id] == frame) || block_in_frustum(sv, Tcw, c.x, c.y, c.z);
             tag = sv.bfresh[id] ? (int)0x80000000 : 0;
         }
         const int pos = warp_append(sv.ctr + C_NVIS, vis);
@@ -216,10 +226,10 @@ __global__ void visible_kernel(const SessionView *svs) {
     }
 }
 
-constexpr int kIntThreads = 128;  // threads per integration CTA (512 / kIntThreads voxels each), 12 CTAs per SM
+constexpr int kIntThreads = 128;  // threads per integration CTA (512 / kIntThreads voxels each), 16 CTAs per SM
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(kIntThreads, 12) integrate_kernel(const SessionView *svs, int mode) {
+__global__ void __launch_bounds__(kIntThreads, 16) integrate_kernel(const SessionView *svs, int mode) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || sv.layout != LAYOUT) return;
     __shared__ M34 Tcw_s;
@@ -316,7 +326,13 @@ void launch_alloc_visible(const SessionView *d_sv, int nslots, const Extent &ex,
     const int tiles = ((ex.w + kAllocTile - 1) / kAllocTile) * ((ex.h + kAllocTile - 1) / kAllocTile);
     alloc_kernel<<<dim3(tiles, nslots), kAllocTile * kAllocTile, 0, st>>>(d_sv);
     const int gv = min(max((ex.max_pool + 255) / 256, 1), 1216);
-    visible_kernel<<<dim3(gv, nslots), 256, 0, st>>>(d_sv);
+    visible_kernel<true><<<dim3(gv, nslots), 256, 0, st>>>(d_sv);
+}
+
+void launch_visible_frustum(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {
+    vis_begin_kernel<<<nslots, 32, 0, st>>>(d_sv);
+    const int gv = min(max((ex.max_pool + 255) / 256, 1), 1216);
+    visible_kernel<false><<<dim3(gv, nslots), 256, 0, st>>>(d_sv);
 }
 
 void launch_integrate(const SessionView *d_sv, int nslots, const Extent &ex, int mode, const int *layouts,

@@ -210,7 +210,7 @@ constexpr int kRayTileW = 8, kRayTileH = 8;  // 8x4-pixel warps: coherent march 
 constexpr int kMaxMarch = 1 << 16;  // safety bound; the march advances >= 1 voxel per step
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(kRayTileW *kRayTileH) raycast_kernel(const SessionView *svs, float4 *vmap_ext,
+__global__ void __launch_bounds__(kRayTileW *kRayTileH, 24) raycast_kernel(const SessionView *svs, float4 *vmap_ext,
                                                                        long long vmap_pitch) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || sv.layout != LAYOUT) return;

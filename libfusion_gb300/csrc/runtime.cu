@@ -566,6 +566,50 @@ GBF_API gbf_status gbf_raycast(gbf_session *s, const double T[16], float *vmap, 
     return check_cuda("gbf_raycast");
 }
 
+GBF_API gbf_status gbf_raycast_check_visibility(gbf_session *s, const double T[16], float *vmap, int64_t vmap_pitch,
+                                                void *stream) {
+    if (!s || !T || !vmap) return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast_check_visibility: null");
+    if (vmap_pitch < s->K.width * 16)
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast_check_visibility: pitch smaller than a row");
+    cudaStream_t st = (cudaStream_t)stream;
+    gbf_status r = set_map_pose(s, T, st);
+    if (r != GBF_OK) return r;
+    launch_visible_frustum(s->d_view, 1, s->ex, st);
+    launch_raycast(s->d_view, 1, s->ex, reinterpret_cast<float4 *>(vmap), vmap_pitch, 0, s->layouts, st);
+    return check_cuda("gbf_raycast_check_visibility");
+}
+
+GBF_API gbf_status gbf_render_scene(const float *vmap, int64_t vmap_pitch, const float *nmap, int64_t nmap_pitch,
+                                    const uint8_t *rgb, int64_t rgb_pitch, int32_t width, int32_t height,
+                                    uint8_t *out, int64_t out_pitch, void *stream) {
+    if (!vmap || !nmap || !out || width < 1 || height < 1)
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_render_scene: null or empty");
+    if (vmap_pitch < width * 16LL || nmap_pitch < width * 16LL || out_pitch < width * 4LL ||
+        (rgb && rgb_pitch < width * 3LL))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_render_scene: pitch smaller than a row");
+    launch_render(reinterpret_cast<const float4 *>(vmap), vmap_pitch, reinterpret_cast<const float4 *>(nmap),
+                  nmap_pitch, rgb, rgb_pitch, 3, width, height, reinterpret_cast<uchar4 *>(out), out_pitch,
+                  (cudaStream_t)stream);
+    return check_cuda("gbf_render_scene");
+}
+
+GBF_API gbf_status gbf_session_render(gbf_session *s, int32_t textured, uint8_t *out, int64_t out_pitch,
+                                      void *stream) {
+    if (!s || !out) return set_error(GBF_ERR_INVALID_ARG, "gbf_session_render: null");
+    const int W = s->K.width, H = s->K.height;
+    if (out_pitch < W * 4LL) return set_error(GBF_ERR_INVALID_ARG, "gbf_session_render: pitch smaller than a row");
+    cudaStream_t st = (cudaStream_t)stream;
+    // the reference frame's maps: the model prediction of the last raycast
+    int idx = 0;
+    cudaError_t e = cudaMemcpyAsync(&idx, &s->view.ts->idx, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "gbf_session_render");
+    launch_render(s->view.vmap[idx][0], W * 16LL, s->view.nmap[idx][0], W * 16LL,
+                  textured ? reinterpret_cast<const uint8_t *>(s->view.rgb4) : nullptr, W * 4LL, 4, W, H,
+                  reinterpret_cast<uchar4 *>(out), out_pitch, st);
+    return check_cuda("gbf_session_render");
+}
+
 GBF_API gbf_status gbf_extract_mesh(gbf_session *s, int32_t mode, float *vtx, void *attr, uint64_t max_tris,
                                     uint64_t *n_tris, void *stream) {
     if (!s || !vtx || !n_tris) return set_error(GBF_ERR_INVALID_ARG, "gbf_extract_mesh: null");

@@ -69,6 +69,8 @@ typedef struct or_system_f64 or_system_f64;
     int or_fuse_##S(or_map_##S *m, const float *depth, const uint8_t *rgb, const float *nmap, const double T[16]); \
     /* DenseMapping::raycast: z-range tiles of the last fuse's visible blocks + march; vmap float4 */              \
     int or_raycast_##S(or_map_##S *m, const double T[16], float *vmap);                                            \
+    /* DenseMapping::raycast_check_visibility: visible list recomputed for T, then raycast */                      \
+    int or_raycast_check_visibility_##S(or_map_##S *m, const double T[16], float *vmap);                           \
     int64_t or_map_blocks_##S(const or_map_##S *m);                                                                \
     void or_ray_stats_##S(or_map_##S *m, const double T[16], long long out[7], int32_t *steps_per_pixel);            \
     int64_t or_map_export_##S(const or_map_##S *m, int32_t *coords, float *sdf, float *w, uint8_t *rgb,           \
@@ -111,6 +113,9 @@ void or_voxel_to_block(const int v[3], int out[3]);
 void or_voxel_to_local(const int v[3], int out[3]);
 int or_local_idx(const int l[3]);
 int or_tri_table(int cube, int out[16]);   /* fills -1-terminated list, returns count */
+/* renderScene / renderSceneTextured (cuda_imgproc.cu:17-108): float4 camera-frame
+ * vertex / normal maps, rgb8 (NULL = untextured) -> rgba8 */
+void or_render_scene(const float *vmap, const float *nmap, const uint8_t *rgb, int w, int h, uint8_t *out);
 int or_edge_table(int cube);
 short or_pack_sdf(float v);
 float or_unpack_sdf(short v);

@@ -63,6 +63,7 @@ def lib() -> C.CDLL:
                 f"or_map_destroy_{s}": (None, [P]),
                 f"or_fuse_{s}": (C.c_int, [P, P, P, P, D]),
                 f"or_raycast_{s}": (C.c_int, [P, D, P]),
+                f"or_raycast_check_visibility_{s}": (C.c_int, [P, D, P]),
                 f"or_map_blocks_{s}": (C.c_int64, [P]),
                 f"or_ray_stats_{s}": (None, [P, D, C.POINTER(C.c_longlong), P]),
                 f"or_map_export_{s}": (C.c_int64, [P, P, P, P, P, C.c_int64]),
@@ -106,6 +107,8 @@ def lib() -> C.CDLL:
         L.or_pack_sdf.argtypes = [C.c_float]
         L.or_unpack_sdf.restype = C.c_float
         L.or_unpack_sdf.argtypes = [C.c_short]
+        L.or_render_scene.restype = None
+        L.or_render_scene.argtypes = [P, P, P, C.c_int, C.c_int, P]
         _lib = L
     return _lib
 
@@ -157,6 +160,13 @@ class OracleMap:
         if vmap is None:
             vmap = np.full((self.K.height, self.K.width, 4), np.nan, np.float32)
         self.fn("or_raycast")(self.h, _d16(pose), _p(vmap))
+        return vmap
+
+    def raycast_check_visibility(self, pose, vmap: np.ndarray | None = None) -> np.ndarray:
+        """DenseMapping::raycast_check_visibility: visible list for `pose`, then raycast."""
+        if vmap is None:
+            vmap = np.full((self.K.height, self.K.width, 4), np.nan, np.float32)
+        self.fn("or_raycast_check_visibility")(self.h, _d16(pose), _p(vmap))
         return vmap
 
     def ray_stats(self, pose, per_pixel: bool = False):
@@ -348,3 +358,15 @@ def ref_find_entry(dump: dict, pos) -> int:
         if e["offset"] <= 0:
             return -1
         i = nbk + int(e["offset"]) - 1
+
+
+def render_scene(vmap: np.ndarray, nmap: np.ndarray, rgb: np.ndarray | None = None) -> np.ndarray:
+    """renderScene / renderSceneTextured (cuda_imgproc.cu:17-108): (H, W, 4) float32
+    camera-frame vertex and normal maps, optional (H, W, 3) uint8 colour -> (H, W, 4) uint8."""
+    h, w = vmap.shape[:2]
+    vmap = np.ascontiguousarray(vmap, np.float32)
+    nmap = np.ascontiguousarray(nmap, np.float32)
+    out = np.zeros((h, w, 4), np.uint8)
+    c = None if rgb is None else np.ascontiguousarray(rgb, np.uint8)
+    lib().or_render_scene(_p(vmap), _p(nmap), _p(c), w, h, _p(out))
+    return out

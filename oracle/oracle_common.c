@@ -77,3 +77,54 @@ int or_tri_table(int cube, int out[16]) {
     for (int i = 0; i < n; ++i) out[i] = (int)((p >> (4 + 4 * i)) & 0xF);
     return n;
 }
+
+/* ---- renderPoint / renderSceneK / renderSceneTexturedK (cuda_imgproc.cu:17-108) ---- */
+
+typedef struct { float x, y, z; } F3;
+
+static F3 f3(float x, float y, float z) { F3 v = {x, y, z}; return v; }
+/* Vector3::operator* (dot, vector_type.h:83-86) and norm (:98-101) */
+static float f3_dot(F3 a, F3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+/* normalised(V) = V / V.norm() (vector_type.h:198-201) */
+static F3 f3_normalised(F3 v) {
+    const float n = sqrtf((v.x * v.x + v.y * v.y) + v.z * v.z);
+    return f3(v.x / n, v.y / n, v.z / n);
+}
+/* __saturatef(x) * 255.f, then static_cast<unsigned char> */
+static uint8_t sat255(float v) {
+    const float s = (v != v) ? 0.f : (v < 0.f ? 0.f : (v > 1.f ? 1.f : v));
+    return (uint8_t)(s * 255.f);
+}
+
+static void render_point(F3 p, F3 n, F3 img, F3 light, uint8_t out[4]) {
+    float c0 = 4.f / 255.f, c1 = 2.f / 255.f, c2 = 2.f / 255.f;
+    if (!(p.x != p.x)) {
+        const float Ka = 0.3f, Kd = 0.5f, Ks = 0.2f, sp = 20.f;
+        const float Ax = img.x, Dx = img.y, Sx = img.z, Lx = 1.f;
+        const F3 L = f3_normalised(f3(light.x - p.x, light.y - p.y, light.z - p.z));
+        const F3 V = f3_normalised(f3(0.f - p.x, 0.f - p.y, 0.f - p.z));
+        /* 2 * normal: operator*(T S, Vector3<U> V) with T = int returns Vector3<int>,
+         * truncating 2 n to integers (vector_type.h:168-172); then * (normal * L) as float */
+        const float nl = f3_dot(n, L);
+        const int tx = or_trunc_sat(n.x * 2.f), ty = or_trunc_sat(n.y * 2.f), tz = or_trunc_sat(n.z * 2.f);
+        const F3 R = f3_normalised(f3((float)tx * nl - L.x, (float)ty * nl - L.y, (float)tz * nl - L.z));
+        const float rv = f3_dot(R, V);
+        const float Ix = ((Ax * Ka) * Dx + ((Lx * Kd) * Dx) * fmaxf(0.f, nl)) + ((Lx * Ks) * Sx) * powf(fmaxf(0.f, rv), sp);
+        c0 = c1 = c2 = Ix;
+    }
+    out[0] = sat255(c0);
+    out[1] = sat255(c1);
+    out[2] = sat255(c2);
+    out[3] = 255;
+}
+
+void or_render_scene(const float *vmap, const float *nmap, const uint8_t *rgb, int w, int h, uint8_t *out) {
+    const F3 light = f3(5.f, 5.f, 5.f);
+    for (int i = 0; i < w * h; ++i) {
+        const F3 p = f3(vmap[4 * i], vmap[4 * i + 1], vmap[4 * i + 2]);
+        const F3 n = f3(nmap[4 * i], nmap[4 * i + 1], nmap[4 * i + 2]);
+        const F3 img = rgb ? f3((float)rgb[3 * i] / 255.f, (float)rgb[3 * i + 1] / 255.f, (float)rgb[3 * i + 2] / 255.f)
+                           : f3(1.f, 1.f, 1.f);
+        render_point(p, n, img, light, out + 4 * i);
+    }
+}

@@ -596,6 +596,27 @@ int SFX(or_raycast)(MAP *m, const double T[16], float *vmap) {
     return 1;
 }
 
+/* DenseMapping::raycast_check_visibility (voxel_hashing.cpp:121-135): the visible
+ * list recomputed for pose T by count_visible_entry (ray_tracing.cu:778-807) --
+ * every allocated block with a corner in the frustum (is_block_visible), no
+ * "touched" term -- then raycast at T.  The reference's functor also tests empty
+ * entries and reads an uninitialised entry count (ray_tracing.cu:726-743); only
+ * allocated blocks are taken here. */
+int SFX(or_raycast_check_visibility)(MAP *m, const double T[16], float *vmap) {
+    set_threads(m->cfg.threads);
+    double inv[12];
+    pose_inv(T, inv);
+    const M34 Tcw = to_m(inv);
+    char *v = (char *)malloc((size_t)m->n_used + 1);
+#pragma omp parallel for schedule(static)
+    for (int id = 0; id < m->n_used; ++id) v[id] = block_in_frustum(m, &Tcw, m->bcoord + id * 3);
+    m->nvis = 0;
+    for (int id = 0; id < m->n_used; ++id)
+        if (v[id]) m->vis[m->nvis++] = id;
+    free(v);
+    return SFX(or_raycast)(m, T, vmap);
+}
+
 /* counts of the last fuse's raycast at pose T (single thread): rays marched,
  * march steps, voxel samples (each a hash lookup + one voxel read), trilinear
  * reads, hits */

@@ -265,3 +265,58 @@ def test_session_dump_capacity(gbf, tmp_path):
     m.writeMapToDisk(tmp_path / "y.data", size=(n, n + 4096, 4096))
     with pytest.raises(L.GbfError, match="CAPACITY"):
         small.readMapFromDisk(tmp_path / "y.data")
+
+
+# ---- GPU: block garbage collection (deleteBlock, map_struct.cu:327-363) -----------------------------
+
+
+@pytest.mark.gpu
+def test_delete_and_prune_blocks(gbf):
+    """Deleted blocks leave the map, the others keep their voxels bit for bit, and
+    fusing on from the pruned map equals fusing on from a fresh map holding the
+    kept blocks (a deleted block that is seen again starts from zero)."""
+    import torch
+    L = gbf
+    K, m, T = _fused(L, 0, n=4)
+    c0, s0, w0, r0 = m.export()
+    # explicit deletion of every fifth block
+    gone = c0[::5]
+    assert m.delete_blocks(gone) == len(gone)
+    c1, s1, w1, r1 = m.export()
+    keep = np.ones(len(c0), bool)
+    keep[::5] = False
+    a = H.sort_blocks(c0[keep], s0[keep], w0[keep], r0[keep])
+    b = H.sort_blocks(c1, s1, w1, r1)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    assert m.delete_blocks(gone) == 0  # already gone
+    # radius prune around the camera centre
+    cam = T[:3, 3]
+    bm = 8 * m.cfg.voxel_size
+    centres = (c1 + 0.5) * bm
+    inside = np.linalg.norm(centres - cam, axis=1) <= 1.5
+    assert 0 < inside.sum() < len(c1)
+    assert m.prune(cam, 1.5) == int((~inside).sum())
+    c2, s2, w2, r2 = m.export()
+    a = H.sort_blocks(c1[inside], s1[inside], w1[inside], r1[inside])
+    b = H.sort_blocks(c2, s2, w2, r2)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    # the same blocks imported into a fresh map fuse on identically
+    fresh = L.DenseMapping(K, H.small_config(L, 0))
+    fresh.import_blocks(c2, s2, w2, r2)
+    d, c, T2 = H.frames(L, K, 1, start=14)[0]
+    for mm in (m, fresh):
+        mm.update(H.cuda(H.depth_m(d)), H.cuda(c), T2)
+    torch.cuda.synchronize()
+    a = H.sort_blocks(*m.export())
+    b = H.sort_blocks(*fresh.export())
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    # unobserved blocks: a block imported with zero weights is dropped
+    z = np.array([[9999, 9999, 9999]], np.int32)
+    m.import_blocks(z, np.zeros((1, 512), np.float32), np.zeros((1, 512), np.float32), np.zeros((1, 512, 3), np.uint8))
+    n_before = len(m.export()[0])
+    assert m.prune(drop_unobserved=True) >= 1
+    after = {tuple(x) for x in m.export()[0]}
+    assert (9999, 9999, 9999) not in after and len(after) <= n_before - 1
