@@ -141,6 +141,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# DRAM bytes one pixel-iteration of the ICP + photometric reduction moves, from
+# one ncu capture of a level-0 launch over 4 sessions (100.83 MB for 1,228,800
+# pixel-iterations; profiles/gn_reduce_kernel_4x640x480.md): the roofline's traffic
+REDUCE_DRAM_BYTES_PER_PIXEL_ITER = 100.828160e6 / 1228800
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -369,18 +375,23 @@ def run_ours(args):
     bad = [i for i, st in enumerate(status) if st.status & ~L.FLAG_TRACK_FAILED]
     failed = sum(1 for st in status if st.status & L.FLAG_TRACK_FAILED)
 
-    # roofline of the dominant kernel phase
+    # roofline of the dominant kernel phase: algorithmic bytes of the work the
+    # phase's launches did, over their CUDA-event time (the mean launch)
     dom = max(("integrate", "track"), key=lambda n: phases[n])
     peak, peak_kind = measured_peaks()
-    bytes_launch = kernel_bytes(L, sessions, dom, K, pi1 - pi0, ib1 - ib0, phases["ticks"])
+    bytes_step = kernel_bytes(L, sessions, dom, K, pi1 - pi0, ib1 - ib0, phases["ticks"])
     n_launch = 1 if dom == "integrate" else sum(sessions[0].cfg.max_iterations[l] for l in range(3))
-    achieved = bytes_launch / (phases[dom] / 1e3) / 1e9
+    achieved = bytes_step / (phases[dom] / 1e3) / 1e9
+    pix_iter = (pi1 - pi0) / phases["ticks"]
+    traffic = REDUCE_DRAM_BYTES_PER_PIXEL_ITER * pix_iter / n_launch if dom == "track" else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "integrate_kernel" if dom == "integrate" else "gn_reduce_kernel",
+                "traffic": traffic, "kernel": "integrate_kernel" if dom == "integrate" else "gn_reduce_kernel",
                 "launches_per_step": n_launch, "peak_source": f"{peak_kind} hbm_gbs",
-                "algorithmic_bytes_per_step": bytes_launch,
-                "work_per_step": {"pixel_iterations": (pi1 - pi0) / phases["ticks"],
-                                  "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
+                "algorithmic_bytes_per_launch": bytes_step / n_launch, "algorithmic_bytes_per_step": bytes_step,
+                "traffic_basis": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0 launch at 4 "
+                                 "sessions (profiles/gn_reduce_kernel_4x640x480.md): 82.05 B per pixel-iteration, "
+                                 "times this run's pixel-iterations per launch" if traffic is not None else None,
+                "work_per_step": {"pixel_iterations": pix_iter, "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
                 "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream"}
 
     # ---- end to end through the public API with host buffers (pinned): the same

@@ -321,17 +321,22 @@ void launch_fuse_import(const SessionView *d_sv, const Extent &ex, const FuseImp
     fuse_import_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_sv, in);
 }
 
+// CTAs per session of the visible-block pass (grid-stride over the allocated
+// blocks, whose count only the device knows); enough for a pool's worth
+// without launching a CTA per 256 pool slots
+constexpr int kVisCtas = 152;
+
 void launch_alloc_visible(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {
     fuse_begin_kernel<<<nslots, 32, 0, st>>>(d_sv);
     const int tiles = ((ex.w + kAllocTile - 1) / kAllocTile) * ((ex.h + kAllocTile - 1) / kAllocTile);
     alloc_kernel<<<dim3(tiles, nslots), kAllocTile * kAllocTile, 0, st>>>(d_sv);
-    const int gv = min(max((ex.max_pool + 255) / 256, 1), 1216);
+    const int gv = min(max((ex.max_pool + 255) / 256, 1), kVisCtas);
     visible_kernel<true><<<dim3(gv, nslots), 256, 0, st>>>(d_sv);
 }
 
 void launch_visible_frustum(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {
     vis_begin_kernel<<<nslots, 32, 0, st>>>(d_sv);
-    const int gv = min(max((ex.max_pool + 255) / 256, 1), 1216);
+    const int gv = min(max((ex.max_pool + 255) / 256, 1), kVisCtas);
     visible_kernel<false><<<dim3(gv, nslots), 256, 0, st>>>(d_sv);
 }
 
