@@ -354,6 +354,18 @@ GBF_API gbf_status gbf_batch_results(gbf_batch *b, int32_t back, gbf_slot_result
  * into contiguous groups whose frames run as parallel branches of the tick
  * (graph branches / forked streams).  Results do not depend on it. */
 GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups);
+/* Staggered groups (default off; with 2+ groups): the odd groups run half a
+ * frame out of phase -- each tick they fuse and raycast their previous frame,
+ * then ingest and track the new one -- so one group's tracking shares the GPU
+ * with the other's fusion and raycast.  Each session still runs every step in
+ * order and every result is the same; the poses in gbf_batch_results are those
+ * of the tick's frames, while an odd group's map holds the previous frame until
+ * the next tick or gbf_batch_flush. */
+GBF_API gbf_status gbf_batch_set_stagger(gbf_batch *b, int32_t enable);
+/* Fuse and raycast what the staggered groups owe, and wait: call before reading
+ * a batched session's map (export, mesh, raycast) or driving it alone.  Changing
+ * the slots, groups, stagger or timing, and destroying the batch, flush too. */
+GBF_API gbf_status gbf_batch_flush(gbf_batch *b, void *stream);
 /* Record CUDA events at the phase boundaries of every tick (captured into the
  * graph): ingest, track, alloc+visible, integrate, z-range, march, post. */
 GBF_API gbf_status gbf_batch_set_timing(gbf_batch *b, int32_t enable);

@@ -363,6 +363,14 @@ class FusionBatch:
         return (poses, np.array([x.tracked for x in arr], np.int32), np.array([x.status for x in arr], np.uint32),
                 np.array([x.frame_index for x in arr], np.int64))
 
+    def set_stagger(self, enable: bool) -> None:
+        """Odd session groups half a frame out of phase (same results)."""
+        call("gbf_batch_set_stagger", self._h, 1 if enable else 0)
+
+    def flush(self, stream=None) -> None:
+        """Fuse what the staggered groups owe; call before reading a batched session's map."""
+        call("gbf_batch_flush", self._h, _stream(stream))
+
     def set_groups(self, groups: int) -> None:
         """Run the slots as `groups` concurrent branches of each tick (1..4)."""
         call("gbf_batch_set_groups", self._h, int(groups))

@@ -133,6 +133,8 @@ SIGNATURES = {
     "gbf_batch_set_inputs": (C.c_int, [_P, _I32, _P, _P]),
     "gbf_batch_set_timing": (C.c_int, [_P, _I32]),
     "gbf_batch_set_groups": (C.c_int, [_P, _I32]),
+    "gbf_batch_set_stagger": (C.c_int, [_P, _I32]),
+    "gbf_batch_flush": (C.c_int, [_P, _P]),
     "gbf_batch_stage": (C.c_int, [_P, _I32, _P, _I64, _P, _I64, _P]),
     "gbf_batch_results": (C.c_int, [_P, _I32, _P, _I32]),
     "gbf_batch_phase_ms": (C.c_int, [_P, C.POINTER(C.c_float), _I32]),

@@ -79,6 +79,12 @@ struct gbf_batch {
     gbf_slot_result *d_res[2] = {nullptr, nullptr}; // per-slot results of the tick (device)
     gbf_slot_result *h_res[2] = {nullptr, nullptr}; // pinned copies
     long long submitted = 0;                        // ticks submitted
+    // staggered groups: odd groups run the second half of their previous frame
+    // and then the first half of this one in each tick
+    int stagger = 0;
+    gbf::SessionView *h_views_b[2] = {nullptr, nullptr}; // second-half views (active = half owed)
+    gbf::SessionView *d_views_b = nullptr;
+    std::vector<char> owed;                         // slot owes the second half of its last frame
     static constexpr int kMaxGroups = 4;
     int groups = 2;                                // concurrent session groups per tick
     cudaStream_t side[kMaxGroups - 1] = {};        // branch streams of groups 1..

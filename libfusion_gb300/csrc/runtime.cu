@@ -254,31 +254,56 @@ gbf_status set_map_pose(gbf_session *s, const double T[16], cudaStream_t st) {
 // boundaries are recorded: ingest, track, alloc+visible, integrate, z-range,
 // march, post.
 constexpr int kPhases = 7;
+// Event marks at the phase boundaries (inside a capture an event record must
+// become an event-record node of the graph).
+struct PhaseMarks {
+    cudaEvent_t *ev;
+    bool capturing;
+    PhaseMarks(cudaEvent_t *e, cudaStream_t st) : ev(e), capturing(false) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (ev) cudaStreamIsCapturing(st, &cs);
+        capturing = cs == cudaStreamCaptureStatusActive;
+    }
+    void operator()(int i, cudaStream_t st) const {
+        if (!ev) return;
+        if (capturing) cudaEventRecordWithFlags(ev[i], st, cudaEventRecordExternal);
+        else cudaEventRecord(ev[i], st);
+    }
+};
+
+// First half of a frame: ingest and tracking (the pose of the frame is final
+// after it).
+void enqueue_first_half(const SessionView *d_sv, int nslots, const Extent &ex, const IngestArgs &in, cudaStream_t st,
+                        cudaEvent_t *ev = nullptr) {
+    PhaseMarks mark(ev, st);
+    mark(0, st);
+    launch_ingest(d_sv, nslots, ex, in, st);
+    mark(1, st);
+    launch_track(d_sv, nslots, ex, 1, st);
+    mark(2, st);
+}
+
+// Second half: allocation, visibility, integration and the raycast that makes
+// the next frame's reference maps.
+void enqueue_second_half(const SessionView *d_sv, int nslots, const Extent &ex, const int *layouts, cudaStream_t st,
+                         cudaEvent_t *ev = nullptr) {
+    PhaseMarks mark(ev, st);
+    launch_alloc_visible(d_sv, nslots, ex, st);
+    mark(3, st);
+    launch_integrate(d_sv, nslots, ex, 1, layouts, st);
+    mark(4, st);
+    launch_zrange(d_sv, nslots, ex, st);
+    mark(5, st);
+    launch_march(d_sv, nslots, ex, nullptr, 0, layouts, st);
+    mark(6, st);
+    launch_post(d_sv, nslots, ex, st);
+    mark(7, st);
+}
+
 void enqueue_frame(const SessionView *d_sv, int nslots, const Extent &ex, const int *layouts, const IngestArgs &in,
                    cudaStream_t st, cudaEvent_t *ev = nullptr) {
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (ev) cudaStreamIsCapturing(st, &cs);
-    auto mark = [&](int i) {
-        if (!ev) return;
-        // inside a capture the record must become an event-record node of the graph
-        if (cs == cudaStreamCaptureStatusActive) cudaEventRecordWithFlags(ev[i], st, cudaEventRecordExternal);
-        else cudaEventRecord(ev[i], st);
-    };
-    mark(0);
-    launch_ingest(d_sv, nslots, ex, in, st);
-    mark(1);
-    launch_track(d_sv, nslots, ex, 1, st);
-    mark(2);
-    launch_alloc_visible(d_sv, nslots, ex, st);
-    mark(3);
-    launch_integrate(d_sv, nslots, ex, 1, layouts, st);
-    mark(4);
-    launch_zrange(d_sv, nslots, ex, st);
-    mark(5);
-    launch_march(d_sv, nslots, ex, nullptr, 0, layouts, st);
-    mark(6);
-    launch_post(d_sv, nslots, ex, st);
-    mark(7);
+    enqueue_first_half(d_sv, nslots, ex, in, st, ev);
+    enqueue_second_half(d_sv, nslots, ex, layouts, st, ev);
 }
 
 // kernels launched by enqueue_frame
@@ -835,6 +860,8 @@ GBF_API gbf_status gbf_zrange(gbf_session *s, float *out, int64_t max_cells) {
 
 // ---- batches ------------------------------------------------------------------------
 
+static gbf_status batch_flush(gbf_batch *b, cudaStream_t st);
+
 GBF_API gbf_status gbf_batch_create(int32_t max_sessions, gbf_batch **out) {
     if (!out || max_sessions < 1 || max_sessions > 4096)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_create: 1..4096 sessions");
@@ -845,10 +872,14 @@ GBF_API gbf_status gbf_batch_create(int32_t max_sessions, gbf_batch **out) {
     b->sessions.assign(max_sessions, nullptr);
     b->in_depth.assign(max_sessions, nullptr);
     b->in_rgb.assign(max_sessions, nullptr);
+    b->owed.assign(max_sessions, 0);
     const size_t bytes = sizeof(SessionView) * max_sessions;
     cudaError_t e = cudaMallocHost(&b->h_views[0], bytes);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_views[1], bytes);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_views, bytes);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_views_b[0], bytes);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_views_b[1], bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_views_b, bytes);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev[0], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev[1], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
@@ -871,8 +902,10 @@ GBF_API gbf_status gbf_batch_create(int32_t max_sessions, gbf_batch **out) {
         gbf_batch_destroy(b);
         return cuda_error(e, "gbf_batch_create");
     }
-    memset(b->h_views[0], 0, bytes);
-    memset(b->h_views[1], 0, bytes);
+    for (int k = 0; k < 2; ++k) {
+        memset(b->h_views[k], 0, bytes);
+        memset(b->h_views_b[k], 0, bytes);
+    }
     *out = b;
     return GBF_OK;
 }
@@ -887,13 +920,16 @@ static void batch_invalidate(gbf_batch *b) {
 
 GBF_API gbf_status gbf_batch_destroy(gbf_batch *b) {
     if (!b) return GBF_OK;
+    if (b->d_views_b) batch_flush(b, nullptr);  // the sessions outlive the batch: fuse what is owed
     cudaDeviceSynchronize();
     batch_invalidate(b);
     for (int k = 0; k < 2; ++k) {
         if (b->h_views[k]) cudaFreeHost(b->h_views[k]);
+        if (b->h_views_b[k]) cudaFreeHost(b->h_views_b[k]);
         if (b->ev[k]) cudaEventDestroy(b->ev[k]);
     }
     if (b->d_views) cudaFree(b->d_views);
+    if (b->d_views_b) cudaFree(b->d_views_b);
     if (b->own) cudaStreamDestroy(b->own);
     for (int g = 0; g < gbf_batch::kMaxGroups - 1; ++g) {
         if (b->side[g]) cudaStreamDestroy(b->side[g]);
@@ -918,6 +954,8 @@ GBF_API gbf_status gbf_batch_destroy(gbf_batch *b) {
 
 GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
     if (!b || slot < 0 || slot >= b->max_slots) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set: bad slot");
+    gbf_status fs = batch_flush(b, nullptr);
+    if (fs != GBF_OK) return fs;
     // a previous tick may still read the mirrors
     for (int k = 0; k < 2; ++k)
         if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
@@ -965,10 +1003,17 @@ static void batch_results(gbf_batch *b, int k, cudaStream_t st) {
     cudaMemcpyAsync(b->h_res[k], b->d_res[k], sizeof(gbf_slot_result) * b->nslots, cudaMemcpyDeviceToHost, st);
 }
 
+static int effective_groups(const gbf_batch *b) { return b->timing ? 1 : std::min(b->groups, b->nslots); }
+static bool staggered(const gbf_batch *b) { return b->stagger && effective_groups(b) >= 2; }
+static int group_lo(const gbf_batch *b, int g, int groups) { return b->nslots * g / groups; }
+
 static void batch_enqueue(gbf_batch *b, int k, cudaStream_t st) {
     cudaMemcpyAsync(b->d_views, b->h_views[k], sizeof(SessionView) * b->nslots, cudaMemcpyHostToDevice, st);
     IngestArgs a{0, 0, nullptr, 0, nullptr, 0};
-    const int groups = b->timing ? 1 : std::min(b->groups, b->nslots);
+    const int groups = effective_groups(b);
+    const bool stag = staggered(b);
+    if (stag)
+        cudaMemcpyAsync(b->d_views_b, b->h_views_b[k], sizeof(SessionView) * b->nslots, cudaMemcpyHostToDevice, st);
     if (groups <= 1) {
         enqueue_frame(b->d_views, b->nslots, b->ex, b->layouts, a, st, b->timing ? b->pev[k] : nullptr);
         batch_results(b, k, st);
@@ -977,8 +1022,17 @@ static void batch_enqueue(gbf_batch *b, int k, cudaStream_t st) {
     cudaEventRecord(b->fork, st);
     for (int g = 1; g < groups; ++g) cudaStreamWaitEvent(b->side[g - 1], b->fork, 0);
     for (int g = 0; g < groups; ++g) {
-        const int lo = b->nslots * g / groups, hi = b->nslots * (g + 1) / groups;
-        enqueue_frame(b->d_views + lo, hi - lo, b->ex, b->layouts, a, g == 0 ? st : b->side[g - 1]);
+        const int lo = group_lo(b, g, groups), hi = group_lo(b, g + 1, groups);
+        cudaStream_t gs = g == 0 ? st : b->side[g - 1];
+        if (stag && (g & 1)) {
+            // half a frame out of phase: the previous frame's fusion and raycast,
+            // then this frame's ingest and tracking, so that this group's tracking
+            // runs beside the even groups' fusion and raycast and the other way round
+            enqueue_second_half(b->d_views_b + lo, hi - lo, b->ex, b->layouts, gs);
+            enqueue_first_half(b->d_views + lo, hi - lo, b->ex, a, gs);
+        } else {
+            enqueue_frame(b->d_views + lo, hi - lo, b->ex, b->layouts, a, gs);
+        }
     }
     for (int g = 1; g < groups; ++g) {
         cudaEventRecord(b->join[g - 1], b->side[g - 1]);
@@ -987,9 +1041,49 @@ static void batch_enqueue(gbf_batch *b, int k, cudaStream_t st) {
     batch_results(b, k, st);
 }
 
+// Run the second halves the staggered groups owe (their last frames' fusion and
+// raycast) and wait for them.  Called before anything that changes the slot
+// assignment or the tick layout, and by gbf_batch_flush.
+static gbf_status batch_flush(gbf_batch *b, cudaStream_t st) {
+    bool any = false;
+    for (int i = 0; i < b->nslots; ++i) any = any || b->owed[i];
+    if (!any) return GBF_OK;
+    for (int k = 0; k < 2; ++k)
+        if (b->ev_used[k]) {
+            cudaError_t e = cudaEventSynchronize(b->ev[k]);
+            if (e != cudaSuccess) return cuda_error(e, "gbf_batch_flush: wait");
+        }
+    SessionView *hv = b->h_views_b[0];
+    for (int i = 0; i < b->nslots; ++i) {
+        if (b->owed[i] && b->sessions[i]) {
+            hv[i] = b->sessions[i]->view;
+            hv[i].active = 1;
+        } else {
+            memset(&hv[i], 0, sizeof(SessionView));
+        }
+    }
+    cudaError_t e = cudaMemcpyAsync(b->d_views_b, hv, sizeof(SessionView) * b->nslots, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_error(e, "gbf_batch_flush");
+    enqueue_second_half(b->d_views_b, b->nslots, b->ex, b->layouts, st);
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "gbf_batch_flush");
+    std::fill(b->owed.begin(), b->owed.end(), 0);
+    return check_cuda("gbf_batch_flush");
+}
+
+GBF_API gbf_status gbf_batch_flush(gbf_batch *b, void *stream) {
+    if (!b) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_flush: null");
+    return batch_flush(b, (cudaStream_t)stream);
+}
+
 GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_t use_graph, void *stream) {
     if (!b || !active) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_process: null");
     if (b->nslots == 0) return GBF_OK;
+    const bool stag = staggered(b);
+    if (!stag) {  // owed halves from a staggered tick run first
+        gbf_status fs = batch_flush(b, (cudaStream_t)stream);
+        if (fs != GBF_OK) return fs;
+    }
     // work goes to `stream` (NULL = legacy default stream); graphs are captured
     // on the batch's own stream because the legacy stream cannot be captured
     cudaStream_t st = (cudaStream_t)stream;
@@ -1019,6 +1113,17 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
             memset(&hv[i], 0, sizeof(SessionView));
         }
     }
+    if (stag) {
+        SessionView *hb = b->h_views_b[k];
+        for (int i = 0; i < b->nslots; ++i) {
+            if (b->owed[i] && b->sessions[i]) {
+                hb[i] = b->sessions[i]->view;
+                hb[i].active = 1;
+            } else {
+                memset(&hb[i], 0, sizeof(SessionView));
+            }
+        }
+    }
     if (use_graph) {
         if (!b->exec[k]) {
             cudaGraph_t g = nullptr;
@@ -1042,6 +1147,12 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
     b->pending[k] = b->timing;
     b->last = k;
     b->submitted += 1;
+    if (stag) {  // odd groups now owe this frame's second half
+        const int groups = effective_groups(b);
+        for (int g = 0; g < groups; ++g)
+            for (int i = group_lo(b, g, groups); i < group_lo(b, g + 1, groups); ++i)
+                b->owed[i] = (g & 1) && b->sessions[i] && active[i];
+    }
     return check_cuda("gbf_batch_process");
 }
 
@@ -1108,6 +1219,8 @@ GBF_API gbf_status gbf_batch_set_inputs(gbf_batch *b, int32_t slot, const uint16
 GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups) {
     if (!b || groups < 1 || groups > gbf_batch::kMaxGroups)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_groups: 1..4 groups");
+    gbf_status fs = batch_flush(b, nullptr);
+    if (fs != GBF_OK) return fs;
     for (int k = 0; k < 2; ++k)
         if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
     if (groups != b->groups) batch_invalidate(b);
@@ -1115,8 +1228,21 @@ GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups) {
     return GBF_OK;
 }
 
+GBF_API gbf_status gbf_batch_set_stagger(gbf_batch *b, int32_t enable) {
+    if (!b) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_stagger: null");
+    gbf_status fs = batch_flush(b, nullptr);
+    if (fs != GBF_OK) return fs;
+    for (int k = 0; k < 2; ++k)
+        if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
+    if ((enable ? 1 : 0) != b->stagger) batch_invalidate(b);
+    b->stagger = enable ? 1 : 0;
+    return GBF_OK;
+}
+
 GBF_API gbf_status gbf_batch_set_timing(gbf_batch *b, int32_t enable) {
     if (!b) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_timing: null");
+    gbf_status fs = batch_flush(b, nullptr);
+    if (fs != GBF_OK) return fs;
     for (int k = 0; k < 2; ++k)
         if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
     if (enable && !b->pev[0][0]) {

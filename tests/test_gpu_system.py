@@ -84,6 +84,7 @@ def test_batch_session_isolation(gbf):
             batch.process([True, True, True, True], use_graph=use_graph)
             torch.cuda.synchronize()
         assert np.array_equal(a.get_camera_pose(), pa)
+        batch.flush()  # the staggered group's last frame is fused here
         mb = a.export()
         for x, y in zip(ma, mb):
             xs = H.sort_blocks(ma[0], x)[1]
@@ -125,6 +126,7 @@ def test_batch_staging_pipeline_matches_session_staging(gbf):
             if pipelined and k > 0:
                 seen.append(b.results(back=1))
         last = b.results(back=0)
+        b.flush()
         torch.cuda.synchronize()
         poses = [s.get_camera_pose() for s in ss]
         maps = [s.export() for s in ss]
@@ -143,3 +145,47 @@ def test_batch_staging_pipeline_matches_session_staging(gbf):
         assert np.array_equal(last1[0][i], p1[i])
         assert last1[3][i] == 6
     assert [int(r[3][0]) for r in seen] == [1, 2, 3, 4, 5]
+
+
+def test_staggered_groups_same_results(gbf):
+    """Odd groups half a frame out of phase: every tick's poses and, after a
+    flush, every map equal those of the unstaggered batch; changing the layout
+    mid-run (groups, stagger, slot assignment) flushes what is owed first."""
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 1)
+    n = 4
+    fr = [H.frames(L, K, 6, seed=20 + i) for i in range(n)]
+
+    def run(stagger, switch_at=None):
+        ss = [L.System(K, cfg) for _ in range(n)]
+        for s, f in zip(ss, fr):
+            s.set_pose(f[0][2])
+        b = L.FusionBatch(n)
+        for i, s in enumerate(ss):
+            b.set(i, s)
+        b.set_groups(2)
+        b.set_stagger(stagger)
+        poses = []
+        for k in range(6):
+            if switch_at is not None and k == switch_at:
+                b.set_stagger(not stagger)
+            for i, s in enumerate(ss):
+                s.stage(H.cuda(fr[i][k][0]), H.cuda(fr[i][k][1]))
+            b.process([True] * n)
+            poses.append(b.results(back=0)[0])
+        b.flush()
+        torch.cuda.synchronize()
+        maps = [s.export() for s in ss]
+        b.close()
+        return poses, maps
+
+    p0, m0 = run(False)
+    for args in ((True,), (True, 3)):
+        p1, m1 = run(*args)
+        for x, y in zip(p0, p1):
+            assert np.array_equal(x, y)
+        for a, b in zip(m0, m1):
+            for x, y in zip(H.sort_blocks(*a), H.sort_blocks(*b)):
+                assert np.array_equal(x, y)
