@@ -60,6 +60,8 @@ void launch_post(const SessionView *d_sv, int nslots, const Extent &ex, cudaStre
 
 // ---- tracking (tracking.cu) -----------------------------------------------------
 // mode 0: full Gauss-Newton (gbf_track / process frame), stops at the schedule end
+// kernel launches of one launch_track over nslots sessions
+int track_launches(int nslots, const Extent &ex);
 void launch_track(const SessionView *d_sv, int nslots, const Extent &ex, int frame_mode, cudaStream_t st);
 // single reduction for gbf_reduce: pose given as float 3x4 in the kernel args
 void launch_reduce_once(const SessionView *d_sv, const Extent &ex, int level, const float *pose12, float stddev,

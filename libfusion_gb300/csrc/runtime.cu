@@ -307,11 +307,9 @@ void enqueue_frame(const SessionView *d_sv, int nslots, const Extent &ex, const 
 }
 
 // kernels launched by enqueue_frame
-int kernels_per_frame(const Extent &ex, const int *layouts) {
-    int it = 0;
-    for (int l = 0; l < ex.levels; ++l) it += ex.max_iter[l];
+int kernels_per_frame(const Extent &ex, const int *layouts, int nslots) {
     const int nl = layouts[0] + layouts[1];
-    return (1 + (ex.levels - 1) + 1) + (2 + it) + 3 + nl + 2 + nl + (ex.levels - 1) + 1;
+    return (1 + (ex.levels - 1) + 1) + track_launches(nslots, ex) + 3 + nl + 2 + nl + (ex.levels - 1) + 1;
 }
 
 }  // namespace
@@ -1276,7 +1274,11 @@ GBF_API gbf_status gbf_batch_phase_ms(gbf_batch *b, float *ms, int32_t n) {
 
 GBF_API gbf_status gbf_batch_kernels(gbf_batch *b, int32_t *n) {
     if (!b || !n) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_kernels: null");
-    *n = b->nslots ? kernels_per_frame(b->ex, b->layouts) * std::min(b->groups, b->nslots) + 1 : 0;
+    int total = 0;
+    const int groups = std::max(1, std::min(b->groups, b->nslots));
+    for (int g = 0; g < groups; ++g)
+        total += kernels_per_frame(b->ex, b->layouts, b->nslots * (g + 1) / groups - b->nslots * g / groups);
+    *n = b->nslots ? total + 1 : 0;
     return GBF_OK;
 }
 

@@ -549,15 +549,29 @@ __global__ void track_finish_kernel(const SessionView *svs, int frame_mode) {
 
 }  // namespace
 
+// Sessions whose Gauss-Newton iterations run back to back before the next
+// subgroup's: a subgroup's level-0 images (about 25 MB per 640x480 session)
+// then stay in L2 from one iteration to the next.
+constexpr int kTrackSubgroup = 64;
+
+int track_launches(int nslots, const Extent &ex) {
+    int it = 0;
+    for (int l = 0; l < ex.levels; ++l) it += ex.max_iter[l];
+    return 2 + ((nslots + kTrackSubgroup - 1) / kTrackSubgroup) * it;
+}
+
 void launch_track(const SessionView *d_sv, int nslots, const Extent &ex, int frame_mode, cudaStream_t st) {
     track_begin_kernel<<<nslots, 32, 0, st>>>(d_sv, frame_mode);
     ReduceArgs a{};
     a.once = 0;
-    for (int level = ex.levels - 1; level >= 0; --level) {
-        for (int iter = 0; iter < ex.max_iter[level]; ++iter) {
-            a.level = level;
-            a.iter = iter;
-            gn_reduce_kernel<<<dim3(ex.max_red[level], nslots), kReduceThreads, 0, st>>>(d_sv, a);
+    for (int s0 = 0; s0 < nslots; s0 += kTrackSubgroup) {
+        const int n = min(kTrackSubgroup, nslots - s0);
+        for (int level = ex.levels - 1; level >= 0; --level) {
+            for (int iter = 0; iter < ex.max_iter[level]; ++iter) {
+                a.level = level;
+                a.iter = iter;
+                gn_reduce_kernel<<<dim3(ex.max_red[level], n), kReduceThreads, 0, st>>>(d_sv + s0, a);
+            }
         }
     }
     track_finish_kernel<<<nslots, 32, 0, st>>>(d_sv, frame_mode);
