@@ -44,7 +44,7 @@ struct gbf_session {
     gbf::ArenaLayout lay;
     gbf::SessionView view;            // host copy (active = 1)
     gbf::SessionView *d_view = nullptr; // device copy for single-session launches
-    gbf::Extent ex;
+    gbf::Extent ex{};
     int layouts[2] = {0, 0};
     int device = 0;
 };
@@ -62,7 +62,7 @@ struct gbf_batch {
     cudaStream_t own = nullptr;
     int flip = 0;
     int nslots = 0;
-    gbf::Extent ex;
+    gbf::Extent ex{};
     int layouts[2] = {0, 0};
     int timing = 0;
     int last = -1;

@@ -164,7 +164,7 @@ __device__ __forceinline__ void fuse_weight(const SessionView &sv, int i, float4
     sv.fuse_px[i] = make_float2(ok ? dist : __int_as_float(0x7fffffff), w);
 }
 
-__global__ void level_maps_kernel(const SessionView *svs, int set_sel, int tiles_per_level0) {
+__global__ void __launch_bounds__(256, 8) level_maps_kernel(const SessionView *svs, int set_sel, int tiles_per_level0) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     // flatten the levels: level l owns ceil(P_l / blockDim) CTAs

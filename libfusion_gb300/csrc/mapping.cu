@@ -202,7 +202,7 @@ __global__ void vis_begin_kernel(const SessionView *svs) {
 // flag 2); without it, the frustum test alone (count_visible_entry,
 // ray_tracing.cu:778-807 with VisibleEntryEvaluateFunctor, :681-710).
 template <bool TOUCHED>
-__global__ void visible_kernel(const SessionView *svs) {
+__global__ void __launch_bounds__(256, 6) visible_kernel(const SessionView *svs) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     __shared__ M34 Tcw;

@@ -33,7 +33,7 @@ __global__ void zr_init_kernel(const SessionView *svs) {
     if (blockIdx.x == 0 && threadIdx.x == 0) sv.ctr[C_RENDER] = 0;
 }
 
-__global__ void zrange_kernel(const SessionView *svs) {
+__global__ void __launch_bounds__(256, 6) zrange_kernel(const SessionView *svs) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     __shared__ M34 Tcw;

@@ -959,15 +959,13 @@ GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
         if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
     b->sessions[slot] = s;
     b->staged[0][slot] = b->staged[1][slot] = 0;
-    batch_invalidate(b);
-    b->nslots = 0;
+    int nslots = 0, layouts[2] = {0, 0};
     Extent ex;
     memset(&ex, 0, sizeof(ex));
-    b->layouts[0] = b->layouts[1] = 0;
     for (int i = 0; i < b->max_slots; ++i) {
         gbf_session *t = b->sessions[i];
         if (!t) continue;
-        b->nslots = i + 1;
+        nslots = i + 1;
         ex.w = std::max(ex.w, t->ex.w);
         ex.h = std::max(ex.h, t->ex.h);
         ex.max_pool = std::max(ex.max_pool, t->ex.max_pool);
@@ -976,9 +974,19 @@ GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
             ex.max_red[l] = std::max(ex.max_red[l], t->ex.max_red[l]);
             ex.max_iter[l] = std::max(ex.max_iter[l], t->ex.max_iter[l]);
         }
-        b->layouts[t->cfg.voxel_layout] = 1;
+        layouts[t->cfg.voxel_layout] = 1;
     }
+    // The captured tick reads its sessions from the device views, uploaded every
+    // tick; it depends only on the slot count, the size extents and the voxel
+    // layouts.  A session replaced by one of the same shape (serving churn)
+    // keeps the graphs.
+    if (nslots != b->nslots || memcmp(&ex, &b->ex, sizeof(ex)) != 0 || layouts[0] != b->layouts[0] ||
+        layouts[1] != b->layouts[1])
+        batch_invalidate(b);
+    b->nslots = nslots;
     b->ex = ex;
+    b->layouts[0] = layouts[0];
+    b->layouts[1] = layouts[1];
     return GBF_OK;
 }
 

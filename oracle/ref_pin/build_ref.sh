@@ -1,7 +1,7 @@
 #!/bin/sh
 # Compile the reference's own hash / coordinate / voxel-packing / table code
 # (src/data_struct/map_struct.cu and headers, read where they lie under the
-# reference tree) with the pin driver.  Output only into oracle/_ref/.
+# reference tree) with the pin program.  Output only into oracle/_ref/.
 # Usage: oracle/ref_pin/build_ref.sh [REFERENCE_ROOT]
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)

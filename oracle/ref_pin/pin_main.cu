@@ -1,4 +1,4 @@
-// Pin driver: runs the reference's own host-callable functions (compiled from
+// Pin program: runs the reference's own host-callable functions (compiled from
 // the reference sources where they lie) on a fixed set of inputs and prints
 // the results as JSON for tests/golden.  Built by oracle/ref_pin/build_ref.sh
 // into oracle/_ref/; never part of the product.

@@ -65,4 +65,4 @@ def test_pose_drift_vs_fp64_oracle(gbf):
         o64.process(d, c)
         drift.append(np.abs(s.get_camera_pose()[:3, 3] - o64.pose()[:3, 3]).max())
     print(f"pose drift vs FP64 oracle over {len(fr)} frames: max {max(drift)*1e3:.3f} mm")
-    assert max(drift) < 1e-3  # the benchmark spec's bound: 1 mm
+    assert max(drift) < 1e-3  # the target bound: 1 mm
