@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--groups", type=int, default=2, help="concurrent session groups per tick")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--serve-ticks", type=int, default=60, help="ticks of the churn (arrival / eviction) run")
+    ap.add_argument("--serve-ticks", type=int, default=120, help="ticks of the churn (arrival / eviction) run")
     return ap.parse_args()
 
 
