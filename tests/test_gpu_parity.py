@@ -223,3 +223,41 @@ def test_mesh_clamps_to_capacity(gbf):
     m.update(H.cuda(H.depth_m(d)), H.cuda(c), T)
     vtx = torch.zeros((100, 3, 3), dtype=torch.float32, device="cuda")
     assert m.fetch_mesh_vertex_only(vtx) == 100
+
+
+@pytest.mark.parametrize("w,h", [(328, 248), (1280, 720)])
+def test_ragged_and_largest_frames_bit_exact(gbf, w, h):
+    """Frame sizes off the kernels' tile grids (328x248: 32x8 ingest tiles,
+    16x16 allocation tiles and 8x8 raycast tiles all end ragged) and the
+    largest configured resolution (1280x720): fusion, visible sets, z-range and
+    raycast bit-exact against the oracle, and the pyramids' intensity levels."""
+    import oracle as O
+    import torch
+    L = gbf
+    K = H.intrinsics(L, w, h)
+    cfg = H.small_config(L, 0, num_blocks=1 << 17, num_buckets=1 << 18)  # room for every block
+    m = L.DenseMapping(K, cfg)
+    om = _oracle_map(L, cfg, K)
+    fr = H.frames(L, K, 3, step=6)
+    for d, c, T in fr:
+        dm = H.depth_m(d)
+        m.update(H.cuda(dm), H.cuda(c), T)
+        om.fuse(dm, c, T)
+        assert np.array_equal(H.sort_blocks(m.visible_blocks())[0], H.sort_blocks(om.visible())[0])
+    _compare_maps(m.export(), om.export(), exact=True)
+    assert m.stats().status == 0
+    T = fr[-1][2]
+    vm = torch.full((K.height, K.width, 4), float("nan"), device="cuda")
+    m.raycast(vm, T)
+    g, o = vm.cpu().numpy(), om.raycast(T)
+    assert np.array_equal(m.zrange(), om.zrange())
+    gh, oh = ~np.isnan(g[..., 2]), ~np.isnan(o[..., 2])
+    assert np.array_equal(gh, oh) and gh.mean() > 0.8
+    assert np.array_equal(g[gh], o[oh])
+    t = L.DenseTracking(K, H.small_config(L, 0, bilateral=0))
+    of = O.OracleFrame(O.config_from(t.cfg), O.intrinsics_from(K))
+    d, c, _ = fr[0]
+    t.set_reference(H.cuda(H.depth_m(d)), H.cuda(c))
+    of.build(H.depth_m(d), c)
+    for lvl in range(3):
+        assert np.array_equal(t.get_image(1, 2, lvl).cpu().numpy(), of.get(2, lvl))
