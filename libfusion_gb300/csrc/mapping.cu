@@ -14,7 +14,7 @@
 //               stamped this fuse OR a block corner projects into the image
 //               within [zmin, zmax] (is_block_visible, depth_fusion.cu:15-47);
 //               warp-aggregated append to the visible list.
-//   integrate   one CTA per visible block (grid-stride), 2 voxels per thread,
+//   integrate   one CTA per visible block (grid-stride), 4 voxels per thread,
 //               coalesced SoA voxel read-modify-write; blocks allocated this
 //               fuse skip the read and are written whole (lazy zeroing instead
 //               of the reference's full-pool cudaMemset, map_struct.cu:90).
