@@ -32,6 +32,8 @@ struct ArenaLayout {
 gbf_status validate(const gbf_config *cfg, const gbf_intrinsics *K);
 ArenaLayout plan_arena(const gbf_config &cfg, const gbf_intrinsics &K);
 int reduce_ctas(int pixels);
+// reference pixels per reduction CTA at a pyramid level
+int reduce_tile(int level);
 // empty the session's map (table, pool, counters) but keep its pose and tracking state; synchronises
 gbf_status reset_map(gbf_session *s);
 

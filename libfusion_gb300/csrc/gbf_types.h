@@ -22,6 +22,9 @@ constexpr int kCoordBits = 21;          // per block coordinate in the packed ke
 constexpr int kCoordLimit = 1 << 20;    // |block coordinate| must stay below this
 constexpr int kReduceThreads = 256;     // CTA size of the ICP/RGB reduction
 constexpr int kReducePixelsPerThread = 4;
+// pixels per reduction CTA on the pyramid levels above the finest (level 0
+// takes kReduceThreads * kReducePixelsPerThread)
+constexpr int kCoarseReduceTile = 1024;
 constexpr int kReduceWidth = 58;        // 29 ICP + 29 RGB sums
 constexpr int kPartialStride = 64;      // floats per CTA partial record
 
@@ -93,6 +96,7 @@ struct SessionView {
     int max_iter[kMaxLevels];
     LevelK lv[kMaxLevels];
     int red_ctas[kMaxLevels];   // reduction CTAs per level
+    int red_tile[kMaxLevels];   // reference pixels per reduction CTA per level
 
     // map
     HashSlot *table;

@@ -47,6 +47,8 @@ int reduce_ctas(int pixels) {
     return std::max(1, (pixels + per - 1) / per);
 }
 
+int reduce_tile(int level) { return level == 0 ? kReduceThreads * kReducePixelsPerThread : kCoarseReduceTile; }
+
 gbf_status validate(const gbf_config *c, const gbf_intrinsics *K) {
     if (!c || !K) return set_error(GBF_ERR_INVALID_ARG, "null config or intrinsics");
     if (c->num_levels < 1 || c->num_levels > GBF_MAX_LEVELS)
@@ -116,7 +118,10 @@ ArenaLayout plan_arena(const gbf_config &c, const gbf_intrinsics &K) {
     }
     a.zr_min = take((size_t)(K.width / 8) * (K.height / 8) * 4);
     a.zr_max = take((size_t)(K.width / 8) * (K.height / 8) * 4);
-    a.partials = take((size_t)reduce_ctas(K.width * K.height) * kPartialStride * 4);
+    int max_ctas = 1;
+    for (int l = 0, lw = K.width, lh = K.height; l < c.num_levels; ++l, lw /= 2, lh /= 2)
+        max_ctas = std::max(max_ctas, (lw * lh + reduce_tile(l) - 1) / reduce_tile(l));
+    a.partials = take((size_t)max_ctas * kPartialStride * 4);
     a.total = off;
     return a;
 }
@@ -193,7 +198,8 @@ void fill_levels(const gbf_config &c, const gbf_intrinsics &K, SessionView &v) {
         L.fx = fx; L.fy = fy; L.cx = cx; L.cy = cy;
         L.invfx = 1.0f / fx;
         L.invfy = 1.0f / fy;
-        v.red_ctas[l] = reduce_ctas(w * h);
+        v.red_tile[l] = reduce_tile(l);
+        v.red_ctas[l] = std::max(1, (w * h + v.red_tile[l] - 1) / v.red_tile[l]);
         v.max_iter[l] = c.max_iterations[l];
         const float s = 0.5f;
         w = (int)(s * (float)w); h = (int)(s * (float)h);

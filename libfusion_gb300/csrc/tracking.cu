@@ -279,15 +279,15 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 // 128 apart; warp shuffle tree, then a fixed-order pass over the four warps of
 // each half.  Writes 58 floats to part.
 __device__ __forceinline__ void cta_partial(const SessionView &sv, int level, int rs, int cs, const M34 &T,
-                                            float stddev, int cta, float *part) {
+                                            float stddev, int cta, int tile, float *part) {
     __shared__ float warp_sums[kReduceThreads / 32][29];
     __shared__ __align__(16) float4 s_v[kCtaPixels];
     __shared__ __align__(16) float4 s_n[kCtaPixels];
     __shared__ __align__(16) float s_i[kCtaPixels];
     const PhotoConst pc = photo_const(stddev);
     const int P = sv.lv[level].w * sv.lv[level].h;
-    const int first = cta * kCtaPixels;
-    const int n = min(kCtaPixels, P - first);
+    const int first = cta * tile;  // tile <= kCtaPixels, a multiple of 4 (16-byte aligned copies)
+    const int n = min(tile, P - first);
     {
         const float4 *gv = sv.vmap[rs][level] + first, *gn = sv.nmap[rs][level] + first;
         const float *gi = sv.inten[rs][level] + first;
@@ -385,7 +385,8 @@ __global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const Sess
     }
     __syncthreads();
     const int rs = ts->idx, cs = 1 - ts->idx;
-    cta_partial(sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.partials + (size_t)blockIdx.x * kPartialStride);
+    cta_partial(sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.red_tile[level],
+                sv.partials + (size_t)blockIdx.x * kPartialStride);
     __threadfence();
     __syncthreads();
     __shared__ unsigned int ticket;
@@ -650,7 +651,7 @@ __global__ void __launch_bounds__(kReduceThreads, 3) reduce_static_kernel(Sessio
 #pragma unroll
         for (int i = 0; i < 12; ++i) T.m[i] = a.pose[i];
     __syncthreads();
-    cta_partial(sv, 0, 0, 1, T, a.stddev, blockIdx.x, scratch + (size_t)blockIdx.x * kPartialStride);
+    cta_partial(sv, 0, 0, 1, T, a.stddev, blockIdx.x, kCtaPixels, scratch + (size_t)blockIdx.x * kPartialStride);
     __threadfence();
     __syncthreads();
     __shared__ unsigned int ticket;
