@@ -36,6 +36,11 @@ METRIC = "aggregate fused frames/s + p99 frame latency: served vs plain, same GP
 UNIT = "frames/s"
 W, H = 640, 480
 VOXELS = (0.005, 0.006, 0.008, 0.01)  # served sessions draw voxel sizes of 5-10 mm
+# voxel layouts: gbf_voxel_layout value and storage
+LAYOUTS = {"half": (1, "fp16 sdf + binary16 weight + rgba8 (8 B/voxel)"),
+           "snorm": (2, "int16 sdf (rounded) + binary16 weight + rgba8 (8 B/voxel)"),
+           "ref": (0, "int16 sdf (truncated) + f32 weight + rgba8 (12 B/voxel)")}
+LAYOUT = "half"
 
 
 def parse():
@@ -51,6 +56,7 @@ def parse():
     ap.add_argument("--groups", type=int, default=2, help="concurrent session groups per tick")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--serve-ticks", type=int, default=120, help="ticks of the churn (arrival / eviction) run")
+    ap.add_argument("--layout", default="half", choices=sorted(LAYOUTS), help="voxel storage of every session")
     return ap.parse_args()
 
 
@@ -60,7 +66,7 @@ def session_config(L, i: int):
     v = VOXELS[i % len(VOXELS)]
     tau = min(max(3.0 * v, 0.02), 0.03)
     return L.default_config(voxel_size=v, truncation=tau, zmin_update=0.3, zmax_update=4.0, zmin_raycast=0.3,
-                            zmax_raycast=4.0, num_buckets=1 << 19, num_blocks=1 << 18, voxel_layout=L.VOXEL_HALF,
+                            zmax_raycast=4.0, num_buckets=1 << 19, num_blocks=1 << 18, voxel_layout=LAYOUTS[LAYOUT][0],
                             num_levels=3, max_iterations=[10, 5, 3, 3, 3], max_probe=256)
 
 
@@ -68,7 +74,7 @@ def workload_config(sessions: int) -> dict:
     """The served workload both arms report."""
     return {"workload": f"served: {sessions} concurrent 640x480 sessions per GPU, one frame each per tick",
             "sessions_per_gpu": sessions, "voxel_m": list(VOXELS), "truncation": "clip(3*voxel, 2 cm, 3 cm)",
-            "voxel_layout": "fp16 sdf + binary16 weight + rgba8 (8 B/voxel)", "pool_blocks": 1 << 18,
+            "voxel_layout": LAYOUTS[LAYOUT][1], "pool_blocks": 1 << 18,
             "hash_slots": 1 << 19, "pyramid": "3 levels 10/5/3"}
 
 
@@ -179,7 +185,7 @@ def kernel_bytes(L, sessions, phase: str, K, d_pixel_iters: int, d_blocks: int, 
     sessions actually did during the timed ticks (iterations that the
     reference's early-exit rules skipped read nothing)."""
     P = K.width * K.height
-    sv = 8 if sessions[0].cfg.voxel_layout == L.VOXEL_HALF else 12
+    sv = 12 if sessions[0].cfg.voxel_layout == L.VOXEL_REF else 8
     if phase == "integrate":
         # voxel read-modify-write of every visible block + per-pixel depth/weight and colour
         return (2.0 * sv * 512 * d_blocks + len(sessions) * ticks * P * (8 + 4)) / ticks
@@ -569,7 +575,9 @@ def run_ours(args):
 
 
 def main():
+    global LAYOUT
     args = parse()
+    LAYOUT = args.layout
     if args.impl == "reference":
         run_reference(args)
     else:

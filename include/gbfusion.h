@@ -80,7 +80,11 @@ enum {
 typedef enum gbf_voxel_layout {
     GBF_VOXEL_REF = 0,  /* int16 sdf (x32767, truncating) + f32 weight (<=255) + rgb8:
                            the reference Voxel semantics, include/data_struct/voxel.h:11-66 */
-    GBF_VOXEL_HALF = 1  /* fp16 sdf + 16-bit weight (binary16, <=255) + rgb8: 8 B per voxel */
+    GBF_VOXEL_HALF = 1, /* fp16 sdf + 16-bit weight (binary16, <=255) + rgb8: 8 B per voxel */
+    GBF_VOXEL_SNORM = 2 /* int16 sdf (packed as sdf x 32767 rounded to nearest, unpacked as
+                           code x 0x1.000202p-15f, 1/32767 rounded up) + 16-bit weight (binary16,
+                           <=255) + rgb8: 8 B per voxel, a uniform 3.1e-5 sdf step where fp16's
+                           step grows to 4.9e-4 near +-1 */
 } gbf_voxel_layout;
 
 typedef enum gbf_mesh_mode {

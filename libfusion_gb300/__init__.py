@@ -22,13 +22,13 @@ import numpy as np
 
 from . import _lib
 from ._lib import (FLAG_COORD_RANGE, FLAG_HASH_FULL, FLAG_NAN_POSE, FLAG_POOL_EXHAUSTED, FLAG_TRACK_FAILED,
-                   MESH_COLOUR, MESH_NORMAL, MESH_VERTEX, VOXEL_HALF, VOXEL_REF, GbfError, call, default_config, lib,
-                   mat16)
+                   MESH_COLOUR, MESH_NORMAL, MESH_VERTEX, VOXEL_HALF, VOXEL_REF, VOXEL_SNORM, GbfError, call,
+                   default_config, lib, mat16)
 
 __all__ = [
     "IntrinsicMatrix", "DenseMapping", "DenseTracking", "System", "FusionBatch", "SynthScene", "TrackingResult",
     "write_dump", "read_dump", "render_scene",
-    "default_config", "session_bytes", "GbfError", "VOXEL_REF", "VOXEL_HALF", "MESH_VERTEX", "MESH_NORMAL",
+    "default_config", "session_bytes", "GbfError", "VOXEL_REF", "VOXEL_HALF", "VOXEL_SNORM", "MESH_VERTEX", "MESH_NORMAL",
     "MESH_COLOUR", "FLAG_POOL_EXHAUSTED", "FLAG_HASH_FULL", "FLAG_COORD_RANGE", "FLAG_TRACK_FAILED",
     "FLAG_NAN_POSE", "version",
 ]

@@ -23,6 +23,7 @@ FLAG_NAN_POSE = 16
 
 VOXEL_REF = 0
 VOXEL_HALF = 1
+VOXEL_SNORM = 2
 MESH_VERTEX, MESH_NORMAL, MESH_COLOUR = 0, 1, 2
 
 

@@ -162,7 +162,9 @@ __device__ __forceinline__ int find_block(const SessionView &sv, int bx, int by,
 // Voxel storage.  REF: int16 sdf packed as (short)(v*32767) (truncation),
 // unpacked as v/32767.f; float weight clamped to 255 (include/data_struct/
 // voxel.h:36-66).  HALF: fp16 sdf and fp16 weight (clamped to 255), both
-// rounded to nearest.
+// rounded to nearest.  SNORM: int16 sdf packed as v*32767 rounded to nearest and
+// unpacked by one multiply with kSnormUnit, and HALF's fp16 weight.  HALF and
+// SNORM keep sdf (low 16 bits) and weight (high 16 bits) in one 32-bit word.
 struct Vox {
     float sdf;
     float w;
@@ -180,6 +182,24 @@ __device__ __forceinline__ unsigned short weight_half_pack(float w) {
 }
 __device__ __forceinline__ float weight_half_unpack(unsigned short q) { return __half2float(__ushort_as_half(q)); }
 
+// SNORM unit: the float just above 1/32767 (1/32767 rounded up).  A multiply
+// replaces REF's divide, and because code * kSnormUnit * 32767 >= code for every
+// int16 code, both the truncating REF pack (a map dump) and the rounding SNORM
+// pack return the code unchanged.  |sdf| reaches 1 + 2^-23 at code +-32767.
+constexpr float kSnormUnit = 0x1.000202p-15f;
+
+// sdf code of the 32-bit word layouts
+template <int LAYOUT>
+__device__ __forceinline__ float sdf_word_unpack(unsigned short code) {
+    if (LAYOUT == GBF_VOXEL_HALF) return __half2float(__ushort_as_half(code));
+    return (float)(short)code * kSnormUnit;
+}
+template <int LAYOUT>
+__device__ __forceinline__ unsigned sdf_word_pack(float v) {
+    if (LAYOUT == GBF_VOXEL_HALF) return (unsigned)__half_as_ushort(__float2half_rn(v));
+    return (unsigned)(unsigned short)(short)__float2int_rn(v * 32767.f);
+}
+
 // One load gives sdf and weight: HALF packs them in a 32-bit word, REF in 64 bits.
 template <int LAYOUT>
 __device__ __forceinline__ float unpack_sw(unsigned lo, unsigned hi, float &w) {
@@ -188,7 +208,7 @@ __device__ __forceinline__ float unpack_sw(unsigned lo, unsigned hi, float &w) {
         return sdf_ref_unpack((short)(lo & 0xffffu));
     } else {
         w = weight_half_unpack((unsigned short)(lo >> 16));
-        return __half2float(__ushort_as_half((unsigned short)(lo & 0xffffu)));
+        return sdf_word_unpack<LAYOUT>((unsigned short)(lo & 0xffffu));
     }
 }
 
@@ -213,7 +233,7 @@ __device__ __forceinline__ void store_sw_at(void *__restrict__ sw, int i, float 
             make_uint2((unsigned)(unsigned short)sdf_ref_pack(sdf), __float_as_uint(weight_ref_store(w)));
     else
         reinterpret_cast<unsigned *>(sw)[i] =
-            (unsigned)__half_as_ushort(__float2half_rn(sdf)) | ((unsigned)weight_half_pack(w) << 16);
+            sdf_word_pack<LAYOUT>(sdf) | ((unsigned)weight_half_pack(w) << 16);
 }
 
 template <int LAYOUT>
@@ -250,7 +270,7 @@ __device__ __forceinline__ void store_sw(const SessionView &sv, size_t i, float 
             make_uint2((unsigned)(unsigned short)sdf_ref_pack(sdf), __float_as_uint(weight_ref_store(w)));
     } else {
         reinterpret_cast<unsigned *>(sv.vox_sw)[i] =
-            (unsigned)__half_as_ushort(__float2half_rn(sdf)) | ((unsigned)weight_half_pack(w) << 16);
+            sdf_word_pack<LAYOUT>(sdf) | ((unsigned)weight_half_pack(w) << 16);
     }
 }
 

@@ -47,7 +47,7 @@ struct gbf_session {
     gbf::SessionView view;            // host copy (active = 1)
     gbf::SessionView *d_view = nullptr; // device copy for single-session launches
     gbf::Extent ex{};
-    int layouts[2] = {0, 0};
+    int layouts[gbf::kNumLayouts] = {};
     int device = 0;
 };
 
@@ -65,7 +65,7 @@ struct gbf_batch {
     int flip = 0;
     int nslots = 0;
     gbf::Extent ex{};
-    int layouts[2] = {0, 0};
+    int layouts[gbf::kNumLayouts] = {};
     int timing = 0;
     int last = -1;
     cudaEvent_t pev[2][8] = {};   // phase boundaries per mirror (captured into the graphs)

@@ -15,6 +15,7 @@
 namespace gbf {
 
 constexpr int kMaxLevels = 5;
+constexpr int kNumLayouts = 3;         // gbf_voxel_layout values
 constexpr int kBlockSide = 8;
 constexpr int kBlockVoxels = 512;
 constexpr unsigned long long kEmptyKey = ~0ull;

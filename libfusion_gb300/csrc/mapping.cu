@@ -347,6 +347,7 @@ void launch_integrate(const SessionView *d_sv, int nslots, const Extent &ex, int
     const int gi = 152 * 8;
     if (layouts[GBF_VOXEL_REF]) integrate_kernel<GBF_VOXEL_REF><<<dim3(gi, nslots), kIntThreads, 0, st>>>(d_sv, mode);
     if (layouts[GBF_VOXEL_HALF]) integrate_kernel<GBF_VOXEL_HALF><<<dim3(gi, nslots), kIntThreads, 0, st>>>(d_sv, mode);
+    if (layouts[GBF_VOXEL_SNORM]) integrate_kernel<GBF_VOXEL_SNORM><<<dim3(gi, nslots), kIntThreads, 0, st>>>(d_sv, mode);
 }
 
 void launch_fuse(const SessionView *d_sv, int nslots, const Extent &ex, int mode, const int *layouts,

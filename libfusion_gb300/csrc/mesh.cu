@@ -347,13 +347,17 @@ __global__ void __launch_bounds__(kBlockVoxels) mesh_emit_kernel(const SessionVi
 void launch_mesh(const SessionView *d_sv, const Extent &ex, int layout, int mode, float *vtx, void *attr,
                  long long max_tris, int *counts, cudaStream_t st) {
     const int g = min(max(ex.max_pool, 1), 152 * 4);
+    float3 *v3 = reinterpret_cast<float3 *>(vtx);
     if (layout == GBF_VOXEL_REF) mesh_count_kernel<GBF_VOXEL_REF><<<g, kBlockVoxels, 0, st>>>(d_sv, mode, counts);
-    else mesh_count_kernel<GBF_VOXEL_HALF><<<g, kBlockVoxels, 0, st>>>(d_sv, mode, counts);
+    else if (layout == GBF_VOXEL_HALF) mesh_count_kernel<GBF_VOXEL_HALF><<<g, kBlockVoxels, 0, st>>>(d_sv, mode, counts);
+    else mesh_count_kernel<GBF_VOXEL_SNORM><<<g, kBlockVoxels, 0, st>>>(d_sv, mode, counts);
     mesh_scan_kernel<<<1, 1024, 0, st>>>(d_sv, counts);
     if (layout == GBF_VOXEL_REF)
-        mesh_emit_kernel<GBF_VOXEL_REF><<<g, kBlockVoxels, 0, st>>>(d_sv, mode, counts, reinterpret_cast<float3 *>(vtx), attr, max_tris);
+        mesh_emit_kernel<GBF_VOXEL_REF><<<g, kBlockVoxels, 0, st>>>(d_sv, mode, counts, v3, attr, max_tris);
+    else if (layout == GBF_VOXEL_HALF)
+        mesh_emit_kernel<GBF_VOXEL_HALF><<<g, kBlockVoxels, 0, st>>>(d_sv, mode, counts, v3, attr, max_tris);
     else
-        mesh_emit_kernel<GBF_VOXEL_HALF><<<g, kBlockVoxels, 0, st>>>(d_sv, mode, counts, reinterpret_cast<float3 *>(vtx), attr, max_tris);
+        mesh_emit_kernel<GBF_VOXEL_SNORM><<<g, kBlockVoxels, 0, st>>>(d_sv, mode, counts, v3, attr, max_tris);
 }
 
 }  // namespace gbf

@@ -98,7 +98,7 @@ struct BlockCache {
 
 // sdf of pool voxel i (int32 index: the pool is validated to fit), or NaN when
 // unobserved (weight 0).  Only the weight's zero test is needed, so the HALF
-// layout tests its binary16 bits instead of converting them.
+// and SNORM layouts test the binary16 weight bits instead of converting them.
 template <int LAYOUT>
 __device__ __forceinline__ float sdf_at(const SessionView &sv, int i, bool &valid) {
     const float qnan = __int_as_float(0x7fffffff);
@@ -109,7 +109,7 @@ __device__ __forceinline__ float sdf_at(const SessionView &sv, int i, bool &vali
     } else {
         const unsigned q = __ldg(reinterpret_cast<const unsigned *>(sv.vox_sw) + i);
         valid = (q & 0x7fff0000u) != 0u;  // binary16 weight != +-0 (NaN counts as observed, as w != 0.f)
-        return valid ? __half2float(__ushort_as_half((unsigned short)(q & 0xffffu))) : qnan;
+        return valid ? sdf_word_unpack<LAYOUT>((unsigned short)(q & 0xffffu)) : qnan;
     }
 }
 
@@ -347,6 +347,8 @@ void launch_march(const SessionView *d_sv, int nslots, const Extent &ex, float4 
         raycast_kernel<GBF_VOXEL_REF><<<dim3(tiles, nslots), kRayTileW * kRayTileH, 0, st>>>(d_sv, vmap_ext, vmap_pitch);
     if (layouts[GBF_VOXEL_HALF])
         raycast_kernel<GBF_VOXEL_HALF><<<dim3(tiles, nslots), kRayTileW * kRayTileH, 0, st>>>(d_sv, vmap_ext, vmap_pitch);
+    if (layouts[GBF_VOXEL_SNORM])
+        raycast_kernel<GBF_VOXEL_SNORM><<<dim3(tiles, nslots), kRayTileW * kRayTileH, 0, st>>>(d_sv, vmap_ext, vmap_pitch);
 }
 
 void launch_post(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {

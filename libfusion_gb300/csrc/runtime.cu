@@ -64,7 +64,7 @@ gbf_status validate(const gbf_config *c, const gbf_intrinsics *K) {
     if (c->num_buckets < 1 || c->num_blocks < 1) return set_error(GBF_ERR_INVALID_ARG, "table / pool size must be >= 1");
     if ((long long)c->num_blocks * kBlockVoxels > (1ll << 31) - 1)
         return set_error(GBF_ERR_INVALID_ARG, "num_blocks too large (voxel index must fit int32)");
-    if (c->voxel_layout != GBF_VOXEL_REF && c->voxel_layout != GBF_VOXEL_HALF)
+    if (c->voxel_layout < 0 || c->voxel_layout >= kNumLayouts)
         return set_error(GBF_ERR_INVALID_ARG, "unknown voxel layout");
     if (c->max_probe < 1) return set_error(GBF_ERR_INVALID_ARG, "max_probe must be >= 1");
     for (int l = 0; l < c->num_levels; ++l)
@@ -314,7 +314,8 @@ void enqueue_frame(const SessionView *d_sv, int nslots, const Extent &ex, const 
 
 // kernels launched by enqueue_frame
 int kernels_per_frame(const Extent &ex, const int *layouts, int nslots) {
-    const int nl = layouts[0] + layouts[1];
+    int nl = 0;
+    for (int l = 0; l < kNumLayouts; ++l) nl += layouts[l];
     return (1 + (ex.levels - 1) + 1) + track_launches(nslots, ex) + 3 + nl + 2 + nl + (ex.levels - 1) + 1;
 }
 
@@ -772,8 +773,10 @@ GBF_API gbf_status gbf_map_export(gbf_session *s, int32_t *coords, float *sdf, f
         const int cnt = std::min(chunk, n - first);
         if (s->cfg.voxel_layout == GBF_VOXEL_REF)
             export_kernel<GBF_VOXEL_REF><<<std::min(cnt, 1024), 256>>>(s->d_view, first, cnt, d_c, d_s, d_w, d_r);
-        else
+        else if (s->cfg.voxel_layout == GBF_VOXEL_HALF)
             export_kernel<GBF_VOXEL_HALF><<<std::min(cnt, 1024), 256>>>(s->d_view, first, cnt, d_c, d_s, d_w, d_r);
+        else
+            export_kernel<GBF_VOXEL_SNORM><<<std::min(cnt, 1024), 256>>>(s->d_view, first, cnt, d_c, d_s, d_w, d_r);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpy(coords + (size_t)first * 3, d_c, (size_t)cnt * 3 * 4, cudaMemcpyDeviceToHost);
         if (e == cudaSuccess) e = cudaMemcpy(sdf + (size_t)first * kBlockVoxels, d_s, (size_t)cnt * kBlockVoxels * 4, cudaMemcpyDeviceToHost);
@@ -809,8 +812,10 @@ GBF_API gbf_status gbf_map_import(gbf_session *s, const int32_t *coords, const f
         if (e != cudaSuccess) break;
         if (s->cfg.voxel_layout == GBF_VOXEL_REF)
             import_kernel<GBF_VOXEL_REF><<<std::min(cnt, 1024), 256>>>(s->d_view, cnt, d_c, d_s, d_w, d_r);
-        else
+        else if (s->cfg.voxel_layout == GBF_VOXEL_HALF)
             import_kernel<GBF_VOXEL_HALF><<<std::min(cnt, 1024), 256>>>(s->d_view, cnt, d_c, d_s, d_w, d_r);
+        else
+            import_kernel<GBF_VOXEL_SNORM><<<std::min(cnt, 1024), 256>>>(s->d_view, cnt, d_c, d_s, d_w, d_r);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
     }
@@ -965,7 +970,7 @@ GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
         if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
     b->sessions[slot] = s;
     b->staged[0][slot] = b->staged[1][slot] = 0;
-    int nslots = 0, layouts[2] = {0, 0};
+    int nslots = 0, layouts[kNumLayouts] = {};
     Extent ex;
     memset(&ex, 0, sizeof(ex));
     for (int i = 0; i < b->max_slots; ++i) {
@@ -986,13 +991,12 @@ GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
     // tick; it depends only on the slot count, the size extents and the voxel
     // layouts.  A session replaced by one of the same shape (serving churn)
     // keeps the graphs.
-    if (nslots != b->nslots || memcmp(&ex, &b->ex, sizeof(ex)) != 0 || layouts[0] != b->layouts[0] ||
-        layouts[1] != b->layouts[1])
+    if (nslots != b->nslots || memcmp(&ex, &b->ex, sizeof(ex)) != 0 ||
+        memcmp(layouts, b->layouts, sizeof(layouts)) != 0)
         batch_invalidate(b);
     b->nslots = nslots;
     b->ex = ex;
-    b->layouts[0] = layouts[0];
-    b->layouts[1] = layouts[1];
+    memcpy(b->layouts, layouts, sizeof(layouts));
     return GBF_OK;
 }
 

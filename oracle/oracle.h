@@ -36,7 +36,8 @@ typedef struct or_config {
     float voxel_size, truncation;
     float zmin_update, zmax_update, zmin_raycast, zmax_raycast;
     int32_t num_blocks;       /* pool size (blocks past it are not allocated) */
-    int32_t voxel_layout;     /* 0 REF (int16 + f32 weight), 1 HALF (fp16 sdf + fp16 weight) */
+    int32_t voxel_layout;     /* 0 REF (int16 + f32 weight), 1 HALF (fp16 sdf + fp16 weight),
+                                 2 SNORM (int16 rounded to nearest + fp16 weight) */
     int32_t num_levels;
     int32_t max_iterations[OR_MAX_LEVELS];
     float w_icp, w_rgb, icp_dist_thresh, icp_angle_thresh;

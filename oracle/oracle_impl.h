@@ -193,6 +193,7 @@ static inline R vox_sdf(const MAP *m, size_t v) {
     return m->sdf[v];
 #else
     if (m->cfg.voxel_layout == 0) return (float)(int16_t)m->sdf[v] / 32767.f;
+    if (m->cfg.voxel_layout == 2) return (float)(int16_t)m->sdf[v] * 0x1.000202p-15f; /* 1/32767 rounded up */
     _Float16 h;
     memcpy(&h, &m->sdf[v], 2);
     return (float)h;
@@ -217,8 +218,12 @@ static inline void vox_store(MAP *m, size_t v, R sdf, R w) {
         m->sdf[v] = (uint16_t)(int16_t)or_trunc_sat(sdf * 32767.f);
         m->wf[v] = w > 255.f ? 255.f : w;
     } else {
-        _Float16 h = (_Float16)sdf;
-        memcpy(&m->sdf[v], &h, 2);
+        if (m->cfg.voxel_layout == 2) {
+            m->sdf[v] = (uint16_t)(int16_t)or_trunc_sat(rint((double)(sdf * 32767.f))); /* __float2int_rn */
+        } else {
+            _Float16 h = (_Float16)sdf;
+            memcpy(&m->sdf[v], &h, 2);
+        }
         _Float16 hw = (_Float16)(w > 255.f ? 255.f : w);
         memcpy(&m->w16[v], &hw, 2);
     }

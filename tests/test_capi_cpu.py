@@ -49,9 +49,12 @@ def test_session_bytes_and_validation(L):
     n = L.session_bytes(c, K)
     assert n > (1 << 17) * 512 * 10  # voxel pool dominates (REF layout: 10 B / voxel)
     c.voxel_layout = L.VOXEL_HALF
-    assert L.session_bytes(c, K) < n
+    half = L.session_bytes(c, K)
+    assert half < n
+    c.voxel_layout = L.VOXEL_SNORM  # same 8 B per voxel as HALF
+    assert L.session_bytes(c, K) == half
     for bad in (dict(num_levels=0), dict(num_levels=6), dict(voxel_size=0.0), dict(num_blocks=0),
-                dict(voxel_layout=7), dict(max_probe=0)):
+                dict(voxel_layout=3), dict(voxel_layout=-1), dict(max_probe=0)):
         cb = L.default_config(**bad)
         with pytest.raises(L.GbfError):
             L.session_bytes(cb, K)

@@ -16,7 +16,7 @@ def _oracle_map(L, cfg, K):
     return O.OracleMap(O.config_from(cfg), O.intrinsics_from(K))
 
 
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 def test_raycast_check_visibility_bit_exact(gbf, layout):
     """Fuse along the trajectory, then raycast from a pose the last fuse did not
     see from: the visible list is rebuilt for that pose on both sides."""
