@@ -73,7 +73,9 @@ enum {
     GBF_FLAG_POOL_EXHAUSTED = 1u << 0, /* block pool full: blocks were not allocated */
     GBF_FLAG_HASH_FULL      = 1u << 1, /* probe limit hit: blocks were not allocated */
     GBF_FLAG_COORD_RANGE    = 1u << 2, /* block coordinate outside +-2^20            */
-    GBF_FLAG_TRACK_FAILED   = 1u << 3, /* last frame's tracking failed (pose kept)   */
+    GBF_FLAG_TRACK_FAILED   = 1u << 3, /* a frame's tracking failed since the reset
+                                          (pose kept for it); the last frame's result
+                                          is gbf_frame_stats.track.success          */
     GBF_FLAG_NAN_POSE       = 1u << 4  /* solver produced a non-finite pose          */
 };
 
