@@ -516,6 +516,10 @@ def run_ours(args):
                    "host wall clock from the first staging copy to the last tick's results on the host"}
     eb.close()
     del e2e_sessions
+    e2e_pose = {}  # (session, frames processed) -> pose after the served tick
+    for poses_k, _, _, fidx in got:
+        for i in range(S):
+            e2e_pose[(i, int(fidx[i]))] = poses_k[i]
 
     # ---- plain path: one session at a time, one frame at a time, pose read back per frame
     plain_sessions = [L.System(K, session_config(L, i)) for i in range(min(S, 8))]
@@ -523,6 +527,7 @@ def run_ours(args):
         s.set_pose(poses0[i])
     per = max(1, min(args.plain_frames or steps, nfr - warm))
     plat = []
+    plain_pose = {}
     for k in range(warm):  # the served sessions' warm-up frames, untimed
         for i, s in enumerate(plain_sessions):
             d, c = frames[i]
@@ -537,7 +542,7 @@ def run_ours(args):
             d, c = frames[i]
             s.process_images(d[warm + k], c[warm + k])
             b.record(stream)
-            s.get_pose()
+            plain_pose[(i, warm + k + 1)] = s.get_pose()
             plat.append(a.elapsed_time(b))
     torch.cuda.synchronize()
     tp = time.perf_counter() - tp
@@ -549,6 +554,13 @@ def run_ours(args):
              "path": "gbf_process_frame per session, direct launches, pose read back per frame",
              "frame_indices": f"{warm}..{warm + per - 1} after {warm} untimed warm-up frames"}
     del plain_sessions
+    # the same sessions' poses after the same frames, served (in the batch of S) and plain
+    both = sorted(set(e2e_pose) & set(plain_pose))
+    diffs = [float(np.abs(e2e_pose[k] - plain_pose[k]).max()) for k in both]
+    same_results = {"compared": len(both), "max_abs_pose_diff": max(diffs) if diffs else None,
+                    "bit_identical": bool(diffs) and all(np.array_equal(e2e_pose[k], plain_pose[k]) for k in both),
+                    "basis": "camera->world pose of each of the first sessions after the same frame, from the "
+                             "pipelined batch of all sessions (e2e leg) and from the plain one-session path"}
 
     if rank != 0:
         return
@@ -563,7 +575,8 @@ def run_ours(args):
                        inputs="seeded synthetic RGB-D (sphere-traced SDF room, depth noise model) resident in HBM"),
         "latency_ms": {"p50": p(0.50), "p95": p(0.95), "p99": p(0.99), "basis": "tick duration (every session's "
                        "frame arrives at the tick start)"},
-        "plain": plain, "served_vs_plain": value / plain_fps, "serving": serving,
+        "plain": plain, "served_vs_plain": value / plain_fps, "served_vs_plain_results": same_results,
+        "serving": serving,
         "phases_ms": {k: v for k, v in phases.items()},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": kpt * steps,
         "clocks": clk, "tracking_failures": failed, "sessions_with_errors": bad,
