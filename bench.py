@@ -53,7 +53,9 @@ def parse():
     ap.add_argument("--plain-frames", type=int, default=0,
                     help="timed frames per plain session (0 = as many as the timed ticks)")
     ap.add_argument("--no-graph", action="store_true")
-    ap.add_argument("--groups", type=int, default=2, help="concurrent session groups per tick")
+    ap.add_argument("--groups", type=int, default=2, help="concurrent session groups per tick (with --no-autotune)")
+    ap.add_argument("--no-autotune", action="store_true", help="fixed launch shape instead of the batch's tuner")
+    ap.add_argument("--tune-ticks", type=int, default=6, help="timed ticks per tuner candidate")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--serve-ticks", type=int, default=120, help="ticks of the churn (arrival / eviction) run")
     ap.add_argument("--layout", default="half", choices=sorted(LAYOUTS), help="voxel storage of every session")
@@ -76,6 +78,52 @@ def workload_config(sessions: int) -> dict:
             "sessions_per_gpu": sessions, "voxel_m": list(VOXELS), "truncation": "clip(3*voxel, 2 cm, 3 cm)",
             "voxel_layout": LAYOUTS[LAYOUT][1], "pool_blocks": 1 << 18,
             "hash_slots": 1 << 19, "pyramid": "3 levels 10/5/3"}
+
+
+def tune_launch_shape(L, K, S, frames, poses0, per_candidate):
+    """The batch tuner's search for this workload's shape, run on throwaway
+    sessions of the same configurations over the first frames, so that the
+    measured batches settle from the process-wide table at their first tick."""
+    import torch
+    L.autotune_forget()
+    ss = [L.System(K, session_config(L, i)) for i in range(S)]
+    for i, s in enumerate(ss):
+        s.set_pose(poses0[i])
+    b = L.FusionBatch(S)
+    for i, s in enumerate(ss):
+        b.set(i, s)
+    b.autotune(True, per_candidate)
+    active, k = [True] * S, 0
+    while b.tuning()["state"] != "settled" and k < frames[0][0].shape[0]:
+        for i in range(S):
+            b.set_inputs(i, frames[i][0][k].data_ptr(), frames[i][1][k].data_ptr())
+        b.process(active)
+        k += 1
+    t = b.tuning()
+    t["ticks"] = k
+    b.close()
+    del ss
+    torch.cuda.synchronize()
+    return t
+
+
+def launch_shape(batch, args):
+    if args.no_autotune:
+        batch.set_groups(args.groups)
+    else:
+        batch.autotune(True, args.tune_ticks)
+
+
+def shape_report(batch, tuned, args):
+    t = batch.tuning()
+    if tuned is None:
+        return {"autotune": False, **t["chosen"]}
+    return {"autotune": True, "settled_from_table": t["from_table"], "groups": t["chosen"]["groups"],
+            "stagger": t["chosen"]["stagger"], "ray_tile_w": t["chosen"]["ray_tile_w"],
+            "tuning_ticks": tuned["ticks"], "ticks_per_candidate": tuned["ticks_per_candidate"],
+            "candidates_ms": [[c["groups"], c["stagger"], c["ray_tile_w"], round(c["median_ms"], 3)]
+                              for c in tuned["tried"]],
+            "candidate_fields": ["groups", "stagger", "ray_tile_w", "median tick ms"]}
 
 
 def intrinsics(L):
@@ -391,6 +439,7 @@ def run_ours(args):
         raise SystemExit(f"{S} sessions need {need/2**30:.1f} GiB > 150 GiB budget")
 
     frames, poses0 = render_frames(L, K, replica_seeds(rank, S), nfr)
+    tuned = None if args.no_autotune else tune_launch_shape(L, K, S, frames, poses0, args.tune_ticks)
     sessions = []
     for i in range(S):
         s = L.System(K, session_config(L, i))
@@ -399,7 +448,7 @@ def run_ours(args):
     batch = L.FusionBatch(S)
     for i, s in enumerate(sessions):
         batch.set(i, s)
-    batch.set_groups(args.groups)
+    launch_shape(batch, args)
     active = [True] * S
     use_graph = not args.no_graph
     stream = torch.cuda.Stream()
@@ -488,7 +537,7 @@ def run_ours(args):
     eb = L.FusionBatch(S)
     for i, s in enumerate(e2e_sessions):
         eb.set(i, s)
-    eb.set_groups(args.groups)
+    launch_shape(eb, args)
     copy = torch.cuda.Stream()
     got = []
 
@@ -570,7 +619,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warm,
         "ms_per_step": total_ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": dict(workload_config(S), graph=use_graph, session_groups=args.groups,
+        "config": dict(workload_config(S), graph=use_graph, launch_shape=shape_report(batch, tuned, args),
                        l2="working set per tick (voxel pools, 64 x 640x480 pyramids) far above the 129 MB L2; no flush",
                        inputs="seeded synthetic RGB-D (sphere-traced SDF room, depth noise model) resident in HBM"),
         "latency_ms": {"p50": p(0.50), "p95": p(0.95), "p99": p(0.99), "basis": "tick duration (every session's "

@@ -375,6 +375,39 @@ GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups);
  * of the tick's frames, while an odd group's map holds the previous frame until
  * the next tick or gbf_batch_flush. */
 GBF_API gbf_status gbf_batch_set_stagger(gbf_batch *b, int32_t enable);
+/* Raycast tile of the batch's ticks: 64 pixels, tile_w (4, 8, 16 or 32) wide;
+ * default 8 (8x8).  Results do not depend on it. */
+GBF_API gbf_status gbf_batch_set_ray_tile(gbf_batch *b, int32_t tile_w);
+
+/* Online autotuner of the tick's launch shape: session groups (1..4), stagger
+ * (with 2+ groups) and the raycast tile.  These knobs change how a tick is
+ * launched, never what it computes, so the batch tunes while it serves: each
+ * candidate gets ticks_per_candidate ticks, timed with CUDA events on the
+ * submitting stream (the first tick after a switch, which captures a new graph,
+ * is not timed).  The search tries groups x stagger at the 8-wide tile, then the
+ * tile widths at the best of those, and keeps the fastest median.  The choice is
+ * recorded in a process-wide table under the batch's shape (device, slot count,
+ * largest frame size, pool, pyramid and iteration counts, voxel layouts); a batch
+ * of a recorded shape settles from it at its next tick, without exploring, and a
+ * change of shape (gbf_batch_set with another size) looks up or explores again.
+ * Setting groups, stagger or the tile by hand turns the tuner off. */
+#define GBF_TUNE_MAX_REPORT 16
+typedef struct gbf_launch_shape {
+    int32_t groups, stagger, ray_tile_w;
+    float median_ms; /* median timed tick (0: not timed) */
+} gbf_launch_shape;
+typedef struct gbf_tuning {
+    int32_t state;                /* 0 off, 1 exploring, 2 settled                  */
+    int32_t from_table;           /* settled from the process-wide table            */
+    int32_t ticks_per_candidate;
+    gbf_launch_shape chosen;      /* the shape in use                               */
+    int32_t n_tried;              /* candidates timed so far (this batch)          */
+    gbf_launch_shape tried[GBF_TUNE_MAX_REPORT];
+} gbf_tuning;
+GBF_API gbf_status gbf_batch_set_autotune(gbf_batch *b, int32_t enable, int32_t ticks_per_candidate);
+GBF_API gbf_status gbf_batch_tuning(gbf_batch *b, gbf_tuning *out);
+/* Clear the process-wide table of tuned shapes. */
+GBF_API gbf_status gbf_autotune_forget(void);
 /* Fuse and raycast what the staggered groups owe, and wait: call before reading
  * a batched session's map (export, mesh, raycast) or driving it alone.  Changing
  * the slots, groups, stagger or timing, and destroying the batch, flush too. */

@@ -27,7 +27,7 @@ from ._lib import (FLAG_COORD_RANGE, FLAG_HASH_FULL, FLAG_NAN_POSE, FLAG_POOL_EX
 
 __all__ = [
     "IntrinsicMatrix", "DenseMapping", "DenseTracking", "System", "FusionBatch", "SynthScene", "TrackingResult",
-    "write_dump", "read_dump", "render_scene",
+    "write_dump", "read_dump", "render_scene", "autotune_forget",
     "default_config", "session_bytes", "GbfError", "VOXEL_REF", "VOXEL_HALF", "VOXEL_SNORM", "MESH_VERTEX", "MESH_NORMAL",
     "MESH_COLOUR", "FLAG_POOL_EXHAUSTED", "FLAG_HASH_FULL", "FLAG_COORD_RANGE", "FLAG_TRACK_FAILED",
     "FLAG_NAN_POSE", "version",
@@ -367,6 +367,26 @@ class FusionBatch:
         """Odd session groups half a frame out of phase (same results)."""
         call("gbf_batch_set_stagger", self._h, 1 if enable else 0)
 
+    def set_ray_tile(self, tile_w: int) -> None:
+        """Raycast tile of the ticks: 64 pixels, tile_w (4, 8, 16, 32) wide (same results)."""
+        call("gbf_batch_set_ray_tile", self._h, int(tile_w))
+
+    def autotune(self, enable: bool = True, ticks_per_candidate: int = 6) -> None:
+        """Online tuning of groups, stagger and raycast tile while the batch serves
+        (gbf_batch_set_autotune); the choice is kept per batch shape for the process."""
+        call("gbf_batch_set_autotune", self._h, 1 if enable else 0, int(ticks_per_candidate))
+
+    def tuning(self) -> dict:
+        """The tuner's state: 'off' / 'exploring' / 'settled', the shape in use and
+        the median tick time of every candidate timed."""
+        t = _lib.Tuning()
+        call("gbf_batch_tuning", self._h, C.byref(t))
+        shape = lambda s: {"groups": s.groups, "stagger": s.stagger, "ray_tile_w": s.ray_tile_w,
+                           "median_ms": s.median_ms}
+        return {"state": ("off", "exploring", "settled")[t.state], "from_table": bool(t.from_table),
+                "ticks_per_candidate": t.ticks_per_candidate, "chosen": shape(t.chosen),
+                "tried": [shape(t.tried[i]) for i in range(t.n_tried)]}
+
     def flush(self, stream=None) -> None:
         """Fuse what the staggered groups owe; call before reading a batched session's map."""
         call("gbf_batch_flush", self._h, _stream(stream))
@@ -398,6 +418,11 @@ class FusionBatch:
             self.close()
         except Exception:
             pass
+
+
+def autotune_forget() -> None:
+    """Clear the process-wide table of tuned batch shapes (gbf_autotune_forget)."""
+    call("gbf_autotune_forget")
 
 
 def render_scene(vmap, nmap, rgb=None, stream=None):

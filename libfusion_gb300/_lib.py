@@ -77,6 +77,18 @@ class SlotResult(C.Structure):
                 ("frame_index", C.c_int64)]
 
 
+TUNE_MAX_REPORT = 16
+
+
+class LaunchShape(C.Structure):
+    _fields_ = [("groups", C.c_int32), ("stagger", C.c_int32), ("ray_tile_w", C.c_int32), ("median_ms", C.c_float)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("state", C.c_int32), ("from_table", C.c_int32), ("ticks_per_candidate", C.c_int32),
+                ("chosen", LaunchShape), ("n_tried", C.c_int32), ("tried", LaunchShape * TUNE_MAX_REPORT)]
+
+
 class SynthParams(C.Structure):
     _fields_ = [("room", C.c_float * 3), ("n_spheres", C.c_int32), ("n_boxes", C.c_int32),
                 ("sphere_rmin", C.c_float), ("sphere_rmax", C.c_float), ("seed", C.c_uint64),
@@ -135,6 +147,10 @@ SIGNATURES = {
     "gbf_batch_set_timing": (C.c_int, [_P, _I32]),
     "gbf_batch_set_groups": (C.c_int, [_P, _I32]),
     "gbf_batch_set_stagger": (C.c_int, [_P, _I32]),
+    "gbf_batch_set_ray_tile": (C.c_int, [_P, _I32]),
+    "gbf_batch_set_autotune": (C.c_int, [_P, _I32, _I32]),
+    "gbf_batch_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "gbf_autotune_forget": (C.c_int, []),
     "gbf_batch_flush": (C.c_int, [_P, _P]),
     "gbf_batch_stage": (C.c_int, [_P, _I32, _P, _I64, _P, _I64, _P]),
     "gbf_batch_results": (C.c_int, [_P, _I32, _P, _I32]),

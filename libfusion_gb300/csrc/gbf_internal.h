@@ -91,4 +91,20 @@ struct gbf_batch {
     int groups = 2;                                // concurrent session groups per tick
     cudaStream_t side[kMaxGroups - 1] = {};        // branch streams of groups 1..
     cudaEvent_t fork = nullptr, join[kMaxGroups - 1] = {};
+    int ray_tw = 8;                                // raycast tile width (64-pixel tiles)
+    // online autotuner of the launch shape (groups, stagger, raycast tile)
+    struct Shape {
+        int groups, stagger, ray_tw;
+    };
+    int tune_on = 0;                    // gbf_batch_set_autotune
+    int tune_state = 0;                 // 0 idle, 1 exploring, 2 settled
+    int tune_ticks = 6;                 // timed ticks per candidate
+    int tune_stage = 0;                 // 0: groups x stagger at an 8-wide tile, 1: the tile
+    int tune_cur = -1;                  // candidate being timed
+    int tune_skip = 0;                  // ticks left to skip after a switch
+    int tune_cached = 0;                // settled from the process-wide table
+    std::vector<Shape> tune_cand;
+    std::vector<std::vector<float>> tune_ms;  // tick times (ms) per candidate
+    cudaEvent_t tev[2][2] = {};         // per tick parity: start, end of the tick
+    int tick_cand[2] = {-1, -1};        // candidate the tick in flight was timed for
 };

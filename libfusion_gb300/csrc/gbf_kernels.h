@@ -18,7 +18,12 @@ struct Extent {
     int max_red[kMaxLevels]; // largest reduction CTA count per level
     int levels;      // largest level count
     int max_iter[kMaxLevels];
+    int ray_tw;      // raycast tile width (4, 8, 16 or 32 of a 64-pixel tile); 0 = 8
 };
+
+inline int ray_tile_width(const Extent &ex) {
+    return (ex.ray_tw == 4 || ex.ray_tw == 16 || ex.ray_tw == 32) ? ex.ray_tw : 8;
+}
 
 // ---- ingest (ingest.cu) ------------------------------------------------------
 struct IngestArgs {

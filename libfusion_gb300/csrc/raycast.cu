@@ -206,20 +206,24 @@ __device__ __forceinline__ float read_sdf_interped(const SessionView &sv, BlockC
     return (1.0f - fz) * r2 + fz * r3;
 }
 
-constexpr int kRayTileW = 8, kRayTileH = 8;  // 8x4-pixel warps: coherent march lengths
+// One CTA marches a tile of kRayThreads pixels, tw wide and kRayThreads / tw
+// high (tw = 4, 8, 16 or 32; the launch shape is a batch knob).  The default
+// 8x8 tile gives each warp an 8x4 patch: coherent march lengths.
+constexpr int kRayThreads = 64;
 constexpr int kMaxMarch = 1 << 16;  // safety bound; the march advances >= 1 voxel per step
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(kRayTileW *kRayTileH, 24) raycast_kernel(const SessionView *svs, float4 *vmap_ext,
-                                                                       long long vmap_pitch) {
+__global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionView *svs, float4 *vmap_ext,
+                                                                  long long vmap_pitch, int tw) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || sv.layout != LAYOUT) return;
     // the reference skips the raycast when nothing was visible or renderable
     if (sv.ctr[C_NVIS] == 0 || sv.ctr[C_RENDER] == 0) return;
     const LevelK &K = sv.lv[0];
-    const int tiles_x = (K.w + kRayTileW - 1) / kRayTileW;
-    const int x = (blockIdx.x % tiles_x) * kRayTileW + (threadIdx.x % kRayTileW);
-    const int y = (blockIdx.x / tiles_x) * kRayTileH + (threadIdx.x / kRayTileW);
+    const int th = kRayThreads / tw;
+    const int tiles_x = (K.w + tw - 1) / tw;
+    const int x = (blockIdx.x % tiles_x) * tw + (threadIdx.x % tw);
+    const int y = (blockIdx.x / tiles_x) * th + (threadIdx.x / tw);
     __shared__ M34 Twc, Tcw;
     if (threadIdx.x == 0) {
         Tcw = load_m34(sv.ts->map_tcw);
@@ -342,13 +346,15 @@ void launch_zrange(const SessionView *d_sv, int nslots, const Extent &ex, cudaSt
 
 void launch_march(const SessionView *d_sv, int nslots, const Extent &ex, float4 *vmap_ext, long long vmap_pitch,
                   const int *layouts, cudaStream_t st) {
-    const int tiles = ((ex.w + kRayTileW - 1) / kRayTileW) * ((ex.h + kRayTileH - 1) / kRayTileH);
+    const int tw = ray_tile_width(ex), th = kRayThreads / tw;
+    // every slot's tiles fit: a smaller frame has fewer tiles per row and per column
+    const dim3 g(((ex.w + tw - 1) / tw) * ((ex.h + th - 1) / th), nslots);
     if (layouts[GBF_VOXEL_REF])
-        raycast_kernel<GBF_VOXEL_REF><<<dim3(tiles, nslots), kRayTileW * kRayTileH, 0, st>>>(d_sv, vmap_ext, vmap_pitch);
+        raycast_kernel<GBF_VOXEL_REF><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw);
     if (layouts[GBF_VOXEL_HALF])
-        raycast_kernel<GBF_VOXEL_HALF><<<dim3(tiles, nslots), kRayTileW * kRayTileH, 0, st>>>(d_sv, vmap_ext, vmap_pitch);
+        raycast_kernel<GBF_VOXEL_HALF><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw);
     if (layouts[GBF_VOXEL_SNORM])
-        raycast_kernel<GBF_VOXEL_SNORM><<<dim3(tiles, nslots), kRayTileW * kRayTileH, 0, st>>>(d_sv, vmap_ext, vmap_pitch);
+        raycast_kernel<GBF_VOXEL_SNORM><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw);
 }
 
 void launch_post(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {

@@ -14,8 +14,10 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "gbf_device.cuh"
 #include "gbf_internal.h"
@@ -957,6 +959,9 @@ GBF_API gbf_status gbf_batch_destroy(gbf_batch *b) {
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 8; ++i)
             if (b->pev[k][i]) cudaEventDestroy(b->pev[k][i]);
+    for (int k = 0; k < 2; ++k)
+        for (int i = 0; i < 2; ++i)
+            if (b->tev[k][i]) cudaEventDestroy(b->tev[k][i]);
     delete b;
     return check_cuda("gbf_batch_destroy");
 }
@@ -987,13 +992,17 @@ GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
         }
         layouts[t->cfg.voxel_layout] = 1;
     }
+    ex.ray_tw = b->ray_tw;
     // The captured tick reads its sessions from the device views, uploaded every
     // tick; it depends only on the slot count, the size extents and the voxel
     // layouts.  A session replaced by one of the same shape (serving churn)
-    // keeps the graphs.
+    // keeps the graphs, and the tuner keeps its choice.
     if (nslots != b->nslots || memcmp(&ex, &b->ex, sizeof(ex)) != 0 ||
-        memcmp(layouts, b->layouts, sizeof(layouts)) != 0)
+        memcmp(layouts, b->layouts, sizeof(layouts)) != 0) {
         batch_invalidate(b);
+        b->tune_state = 0;  // a new shape: look it up or explore it at the next tick
+        b->tick_cand[0] = b->tick_cand[1] = -1;
+    }
     b->nslots = nslots;
     b->ex = ex;
     memcpy(b->layouts, layouts, sizeof(layouts));
@@ -1092,9 +1101,164 @@ GBF_API gbf_status gbf_batch_flush(gbf_batch *b, void *stream) {
     return batch_flush(b, (cudaStream_t)stream);
 }
 
+// ---------------------------------------------------------------------------
+// Online autotuner of the tick's launch shape.  Its knobs change how a tick is
+// launched, never what it computes: the session groups (parallel branches),
+// staggered groups, and the raycast tile.  While exploring, the batch serves
+// as usual and times each tick with CUDA events on its stream; each candidate
+// gets tune_ticks timed ticks (the first tick after a switch is not timed: it
+// captures and uploads a new graph).  Coordinate search: groups x stagger at
+// the 8-wide tile, then the tile at the best of those.  The fastest median is
+// kept and recorded for the batch's shape in a process-wide table, which later
+// batches of the same shape settle from without exploring.
+
+namespace {
+
+struct TuneKey {
+    int device, nslots;
+    Extent ex;  // ray_tw zeroed
+    int layouts[kNumLayouts];
+};
+
+std::mutex g_tune_mu;
+std::vector<std::pair<TuneKey, gbf_batch::Shape>> g_tune_table;
+
+TuneKey tune_key(const gbf_batch *b) {
+    TuneKey k;
+    memset(&k, 0, sizeof(k));
+    cudaGetDevice(&k.device);
+    k.nslots = b->nslots;
+    k.ex = b->ex;
+    k.ex.ray_tw = 0;
+    memcpy(k.layouts, b->layouts, sizeof(k.layouts));
+    return k;
+}
+
+bool tune_lookup(const gbf_batch *b, gbf_batch::Shape *out) {
+    const TuneKey k = tune_key(b);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    for (const auto &e : g_tune_table)
+        if (memcmp(&e.first, &k, sizeof(k)) == 0) {
+            *out = e.second;
+            return true;
+        }
+    return false;
+}
+
+void tune_store(const gbf_batch *b, const gbf_batch::Shape &c) {
+    const TuneKey k = tune_key(b);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    for (auto &e : g_tune_table)
+        if (memcmp(&e.first, &k, sizeof(k)) == 0) {
+            e.second = c;
+            return;
+        }
+    g_tune_table.emplace_back(k, c);
+}
+
+float median_ms(std::vector<float> v) {
+    if (v.empty()) return FLT_MAX;
+    std::sort(v.begin(), v.end());
+    const size_t n = v.size();
+    return (n & 1) ? v[n / 2] : 0.5f * (v[n / 2 - 1] + v[n / 2]);
+}
+
+int tune_best(const gbf_batch *b) {
+    int best = 0;
+    float best_ms = FLT_MAX;
+    for (size_t i = 0; i < b->tune_cand.size(); ++i) {
+        const float m = median_ms(b->tune_ms[i]);
+        if (m < best_ms) {
+            best_ms = m;
+            best = (int)i;
+        }
+    }
+    return best;
+}
+
+// The time of the tick last recorded on parity k, if it has ended (or, with
+// wait, once it has).
+void tune_collect(gbf_batch *b, int k, bool wait) {
+    const int c = b->tick_cand[k];
+    if (c < 0 || c >= (int)b->tune_ms.size()) return;
+    if (!wait && cudaEventQuery(b->tev[k][1]) != cudaSuccess) return;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, b->tev[k][0], b->tev[k][1]) == cudaSuccess) b->tune_ms[c].push_back(ms);
+    b->tick_cand[k] = -1;
+}
+
+// Switch the launch shape: owed halves run, ticks in flight end, graphs go.
+gbf_status apply_shape(gbf_batch *b, const gbf_batch::Shape &c, cudaStream_t st) {
+    if (c.groups == b->groups && c.stagger == b->stagger && c.ray_tw == b->ray_tw) return GBF_OK;
+    gbf_status fs = batch_flush(b, st);
+    if (fs != GBF_OK) return fs;
+    for (int k = 0; k < 2; ++k)
+        if (b->ev_used[k]) {
+            cudaError_t e = cudaEventSynchronize(b->ev[k]);
+            if (e != cudaSuccess) return cuda_error(e, "gbf_batch autotune: wait");
+            tune_collect(b, k, true);
+        }
+    batch_invalidate(b);
+    b->groups = c.groups;
+    b->stagger = c.stagger;
+    b->ray_tw = c.ray_tw;
+    b->ex.ray_tw = c.ray_tw;
+    return GBF_OK;
+}
+
+gbf_status tune_step(gbf_batch *b, cudaStream_t st) {
+    if (!b->tune_on || b->timing || b->tune_state == 2) return GBF_OK;
+    if (b->tune_state == 0) {
+        gbf_batch::Shape c;
+        if (tune_lookup(b, &c)) {
+            b->tune_cached = 1;
+            b->tune_state = 2;
+            return apply_shape(b, c, st);
+        }
+        b->tune_cached = 0;
+        b->tune_stage = 0;
+        b->tune_cand.clear();
+        for (int g = 1; g <= std::min(gbf_batch::kMaxGroups, b->nslots); ++g) {
+            b->tune_cand.push_back({g, 0, 8});
+            if (g >= 2) b->tune_cand.push_back({g, 1, 8});
+        }
+        b->tune_ms.assign(b->tune_cand.size(), std::vector<float>());
+        b->tick_cand[0] = b->tick_cand[1] = -1;
+        b->tune_cur = 0;
+        b->tune_skip = 1;
+        b->tune_state = 1;
+        return apply_shape(b, b->tune_cand[0], st);
+    }
+    for (int k = 0; k < 2; ++k) tune_collect(b, k, false);
+    if ((int)b->tune_ms[b->tune_cur].size() < b->tune_ticks) return GBF_OK;
+    b->tune_cur += 1;
+    if (b->tune_cur == (int)b->tune_cand.size()) {
+        const gbf_batch::Shape best = b->tune_cand[tune_best(b)];
+        if (b->tune_stage == 0) {
+            for (int tw : {4, 16, 32}) {
+                b->tune_cand.push_back({best.groups, best.stagger, tw});
+                b->tune_ms.emplace_back();
+            }
+            b->tune_stage = 1;
+        } else {
+            tune_store(b, best);
+            b->tune_state = 2;
+            return apply_shape(b, best, st);
+        }
+    }
+    b->tune_skip = 1;
+    return apply_shape(b, b->tune_cand[b->tune_cur], st);
+}
+
+}  // namespace
+
 GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_t use_graph, void *stream) {
     if (!b || !active) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_process: null");
     if (b->nslots == 0) return GBF_OK;
+    {
+        gbf_status ts = tune_step(b, (cudaStream_t)stream);
+        if (ts != GBF_OK) return ts;
+    }
     const bool stag = staggered(b);
     if (!stag) {  // owed halves from a staggered tick run first
         gbf_status fs = batch_flush(b, (cudaStream_t)stream);
@@ -1109,6 +1273,7 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
         cudaError_t e = cudaEventSynchronize(b->ev[k]);
         if (e != cudaSuccess) return cuda_error(e, "gbf_batch_process: wait");
         if (b->timing && b->pending[k]) harvest(b, k);
+        tune_collect(b, k, true);
     }
     SessionView *hv = b->h_views[k];
     for (int i = 0; i < b->nslots; ++i) {
@@ -1140,6 +1305,18 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
             }
         }
     }
+    // a tick timed for the tuner: events on the submitting stream around it
+    const bool timed = b->tune_on && b->tune_state == 1 && !b->timing;
+    b->tick_cand[k] = -1;
+    if (timed) {
+        if (b->tune_skip > 0) {
+            b->tune_skip -= 1;
+        } else {
+            b->tick_cand[k] = b->tune_cur;
+            cudaError_t e = cudaEventRecord(b->tev[k][0], st);
+            if (e != cudaSuccess) return cuda_error(e, "gbf_batch_process: tuner event");
+        }
+    }
     if (use_graph) {
         if (!b->exec[k]) {
             cudaGraph_t g = nullptr;
@@ -1156,6 +1333,10 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
         if (e != cudaSuccess) return cuda_error(e, "gbf_batch_process: launch");
     } else {
         batch_enqueue(b, k, st);
+    }
+    if (b->tick_cand[k] >= 0) {
+        cudaError_t e = cudaEventRecord(b->tev[k][1], st);
+        if (e != cudaSuccess) return cuda_error(e, "gbf_batch_process: tuner event");
     }
     cudaError_t e = cudaEventRecord(b->ev[k], st);
     if (e != cudaSuccess) return cuda_error(e, "gbf_batch_process: record");
@@ -1232,6 +1413,13 @@ GBF_API gbf_status gbf_batch_set_inputs(gbf_batch *b, int32_t slot, const uint16
     return GBF_OK;
 }
 
+// A launch-shape knob set by hand ends the tuner's control of the batch.
+static void tune_off(gbf_batch *b) {
+    b->tune_on = 0;
+    b->tune_state = 0;
+    b->tick_cand[0] = b->tick_cand[1] = -1;
+}
+
 GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups) {
     if (!b || groups < 1 || groups > gbf_batch::kMaxGroups)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_groups: 1..4 groups");
@@ -1239,6 +1427,7 @@ GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups) {
     if (fs != GBF_OK) return fs;
     for (int k = 0; k < 2; ++k)
         if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
+    tune_off(b);
     if (groups != b->groups) batch_invalidate(b);
     b->groups = groups;
     return GBF_OK;
@@ -1250,8 +1439,77 @@ GBF_API gbf_status gbf_batch_set_stagger(gbf_batch *b, int32_t enable) {
     if (fs != GBF_OK) return fs;
     for (int k = 0; k < 2; ++k)
         if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
+    tune_off(b);
     if ((enable ? 1 : 0) != b->stagger) batch_invalidate(b);
     b->stagger = enable ? 1 : 0;
+    return GBF_OK;
+}
+
+GBF_API gbf_status gbf_batch_set_ray_tile(gbf_batch *b, int32_t tile_w) {
+    if (!b || (tile_w != 4 && tile_w != 8 && tile_w != 16 && tile_w != 32))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_ray_tile: tile width 4, 8, 16 or 32");
+    gbf_status fs = batch_flush(b, nullptr);
+    if (fs != GBF_OK) return fs;
+    for (int k = 0; k < 2; ++k)
+        if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
+    tune_off(b);
+    if (tile_w != b->ray_tw) batch_invalidate(b);
+    b->ray_tw = tile_w;
+    b->ex.ray_tw = tile_w;
+    return GBF_OK;
+}
+
+GBF_API gbf_status gbf_batch_set_autotune(gbf_batch *b, int32_t enable, int32_t ticks_per_candidate) {
+    if (!b) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_autotune: null");
+    if (enable && (ticks_per_candidate < 2 || ticks_per_candidate > 64))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_autotune: 2..64 ticks per candidate");
+    if (!enable) {
+        tune_off(b);
+        return GBF_OK;
+    }
+    for (int k = 0; k < 2; ++k)
+        for (int i = 0; i < 2; ++i)
+            if (!b->tev[k][i]) {
+                cudaError_t e = cudaEventCreate(&b->tev[k][i]);
+                if (e != cudaSuccess) return cuda_error(e, "gbf_batch_set_autotune");
+            }
+    b->tune_on = 1;
+    b->tune_ticks = ticks_per_candidate;
+    b->tune_state = 0;
+    b->tick_cand[0] = b->tick_cand[1] = -1;
+    return GBF_OK;
+}
+
+GBF_API gbf_status gbf_batch_tuning(gbf_batch *b, gbf_tuning *out) {
+    if (!b || !out) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_tuning: null");
+    memset(out, 0, sizeof(*out));
+    out->state = b->tune_on ? b->tune_state : 0;
+    out->from_table = b->tune_on && b->tune_state == 2 ? b->tune_cached : 0;
+    out->chosen.groups = b->groups;
+    out->chosen.stagger = b->stagger;
+    out->chosen.ray_tile_w = b->ray_tw;
+    out->chosen.median_ms = 0.f;
+    out->ticks_per_candidate = b->tune_ticks;
+    if (b->tune_on && !b->tune_cached) {
+        const int n = std::min((int)b->tune_cand.size(), GBF_TUNE_MAX_REPORT);
+        out->n_tried = 0;
+        for (int i = 0; i < n; ++i) {
+            if (b->tune_ms[i].empty()) continue;
+            gbf_launch_shape &t = out->tried[out->n_tried++];
+            t.groups = b->tune_cand[i].groups;
+            t.stagger = b->tune_cand[i].stagger;
+            t.ray_tile_w = b->tune_cand[i].ray_tw;
+            t.median_ms = median_ms(b->tune_ms[i]);
+            if (t.groups == b->groups && t.stagger == b->stagger && t.ray_tile_w == b->ray_tw)
+                out->chosen.median_ms = t.median_ms;
+        }
+    }
+    return GBF_OK;
+}
+
+GBF_API gbf_status gbf_autotune_forget(void) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_table.clear();
     return GBF_OK;
 }
 

@@ -233,3 +233,107 @@ def test_batch_churn_keeps_graph_and_results(gbf):
         for x, y in zip(H.sort_blocks(*s.export()), H.sort_blocks(*m)):
             assert np.array_equal(x, y)
     b.close()
+
+
+def test_autotune_explores_settles_and_keeps_results(gbf):
+    """The online tuner switches groups, stagger and raycast tile while the batch
+    serves: every tick's poses and the final maps equal those of a batch with a
+    fixed launch shape; it settles on the candidate with the fastest median, and
+    a second batch of the same shape settles from the process-wide table."""
+    import torch
+    L = gbf
+    L.autotune_forget()
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 1)
+    n, ticks = 4, 48
+    fr = [H.frames(L, K, ticks, seed=60 + i) for i in range(n)]
+
+    def run(tune):
+        ss = [L.System(K, cfg) for _ in range(n)]
+        for s, f in zip(ss, fr):
+            s.set_pose(f[0][2])
+        b = L.FusionBatch(n)
+        for i, s in enumerate(ss):
+            b.set(i, s)
+        if tune:
+            b.autotune(True, 2)
+        else:
+            b.set_groups(2)
+        poses = []
+        for k in range(ticks):
+            for i, s in enumerate(ss):
+                s.stage(H.cuda(fr[i][k][0]), H.cuda(fr[i][k][1]))
+            b.process([True] * n)
+            poses.append(b.results(back=0)[0])
+        b.flush()
+        torch.cuda.synchronize()
+        t = b.tuning()
+        maps = [s.export() for s in ss]
+        b.close()
+        return poses, maps, t
+
+    p0, m0, t0 = run(False)
+    assert t0["state"] == "off"
+    p1, m1, t1 = run(True)
+    for x, y in zip(p0, p1):
+        assert np.array_equal(x, y)
+    for a, c in zip(m0, m1):
+        for x, y in zip(H.sort_blocks(*a), H.sort_blocks(*c)):
+            assert np.array_equal(x, y)
+    print("tuning:", t1)
+    assert t1["state"] == "settled" and not t1["from_table"]
+    tried = t1["tried"]
+    # groups 1..4 x stagger at the 8-wide tile (7), then tiles 4, 16 and 32 at the best
+    assert len(tried) == 10
+    assert {(c["groups"], c["stagger"]) for c in tried[:7]} == {(1, 0), (2, 0), (2, 1), (3, 0), (3, 1), (4, 0), (4, 1)}
+    assert [c["ray_tile_w"] for c in tried[7:]] == [4, 16, 32]
+    best = min(tried, key=lambda c: c["median_ms"])
+    ch = t1["chosen"]
+    assert (ch["groups"], ch["stagger"], ch["ray_tile_w"]) == (best["groups"], best["stagger"], best["ray_tile_w"])
+    assert all(c["median_ms"] > 0 for c in tried)
+
+    # a batch of the same shape starts from the table
+    ss = [L.System(K, cfg) for _ in range(n)]
+    b = L.FusionBatch(n)
+    for i, s in enumerate(ss):
+        s.set_pose(fr[i][0][2])
+        b.set(i, s)
+    b.autotune(True, 2)
+    for i, s in enumerate(ss):
+        s.stage(H.cuda(fr[i][0][0]), H.cuda(fr[i][0][1]))
+    b.process([True] * n)
+    t2 = b.tuning()
+    assert t2["state"] == "settled" and t2["from_table"]
+    assert t2["chosen"]["groups"] == ch["groups"] and t2["chosen"]["ray_tile_w"] == ch["ray_tile_w"]
+    b.close()
+    L.autotune_forget()
+
+
+@pytest.mark.parametrize("tile_w", [4, 16, 32])
+def test_ray_tile_same_raycast(gbf, tile_w):
+    """A batch's raycast tile width changes the launch, not the vertex maps."""
+    import torch
+    L = gbf
+    K = H.intrinsics(L, 328, 248)  # ragged: no tile shape divides it
+    cfg = H.small_config(L, 1)
+    fr = H.frames(L, K, 3, seed=70)
+    out = []
+    for tw in (8, tile_w):
+        s = L.System(K, cfg)
+        s.set_pose(fr[0][2])
+        b = L.FusionBatch(1)
+        b.set(0, s)
+        b.set_ray_tile(tw)
+        for d, c, _ in fr:
+            s.stage(H.cuda(d), H.cuda(c))
+            b.process([True])
+        b.flush()
+        torch.cuda.synchronize()
+        vm = s.get_image(1, 0, 0)  # the reference set's level-0 vertex map: the last raycast
+        torch.cuda.synchronize()
+        out.append((s.get_camera_pose(), s.export(), vm.cpu().numpy()))
+        b.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    for x, y in zip(H.sort_blocks(*out[0][1]), H.sort_blocks(*out[1][1])):
+        assert np.array_equal(x, y)
+    assert np.array_equal(np.nan_to_num(out[0][2], nan=7.0), np.nan_to_num(out[1][2], nan=7.0))
