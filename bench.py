@@ -265,7 +265,7 @@ def aggregate_rate(sessions_per_rank: int, world: int, steps: int, total_ms: flo
 
 # ----------------------------------------------------------------------------- CPU
 
-def cpu_mix(L, K, warmup: int, steps: int, seconds: float | None = None):
+def cpu_mix(L, K, warmup: int, steps: int, seconds: float | None = None, threads: int | None = None):
     """The FP32 oracle (the reference's kernel bodies restated in C, OpenMP over
     pixels and blocks) on this machine's host cores: one CPU session per voxel
     size of the served mix, `warmup` untimed frames each, then frames timed
@@ -274,7 +274,7 @@ def cpu_mix(L, K, warmup: int, steps: int, seconds: float | None = None):
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     O.build()
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     n_mix = len(VOXELS)
     per = warmup + (steps + n_mix - 1) // n_mix
     mix = []
@@ -304,10 +304,31 @@ def cpu_sample_text(n: int, n_mix: int, threads: int) -> str:
             f"restating the reference kernels, {threads} threads")
 
 
+def cpu_model() -> str:
+    """The host CPU as /proc/cpuinfo names it (x86: model name; Arm: implementer and part)."""
+    info = {}
+    try:
+        for line in open("/proc/cpuinfo"):
+            k, _, v = line.partition(":")
+            info.setdefault(k.strip(), v.strip())
+    except OSError:
+        pass
+    if "model name" in info:
+        return info["model name"]
+    if "CPU part" in info:
+        return f"{os.uname().machine}, CPU implementer {info.get('CPU implementer', '?')} part {info['CPU part']}"
+    return os.uname().machine
+
+
 def cpu_baseline(L, K, seconds: float, warmup: int):
+    """All host threads on the bounded sample, and one thread on a third of it."""
     t, n_mix, threads = cpu_mix(L, K, warmup, 256, seconds)
+    t1, _, _ = cpu_mix(L, K, min(warmup, 2), 256, seconds / 3, threads=1)
     return {"value": len(t) / sum(t), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": cpu_sample_text(len(t), n_mix, threads) + f", {sum(t):.1f} s"}
+            "sample": cpu_sample_text(len(t), n_mix, threads) + f", {sum(t):.1f} s",
+            "cpu": cpu_model(), "nproc": os.cpu_count(),
+            "single_thread": {"value": len(t1) / sum(t1), "unit": UNIT, "cores": 1,
+                              "sample": cpu_sample_text(len(t1), n_mix, 1) + f", {sum(t1):.1f} s"}}
 
 
 def host_frames(L, K, n, seed=0):
