@@ -265,3 +265,58 @@ def test_ragged_and_largest_frames_bit_exact(gbf, w, h):
     of.build(H.depth_m(d), c)
     for lvl in range(3):
         assert np.array_equal(t.get_image(1, 2, lvl).cpu().numpy(), of.get(2, lvl))
+
+
+def test_large_room_figure_eight_bit_exact(gbf):
+    """The large-map configuration: 8x8x3 m room with 20 spheres and 12 boxes,
+    figure-eight path at 0.5 m/s, 640x480, 5 mm voxels, 2 cm truncation,
+    2^21 hash slots and a 2^20-block pool, photometric weight 0.1.  At the
+    ground-truth poses: visible sets per frame, fused map, z-range, raycast and
+    the marching-cubes mesh bit-exact against the oracle; then the tracking
+    loop against the FP32 oracle."""
+    import oracle as O
+    import torch
+    L = gbf
+    K = H.intrinsics(L, 640, 480)
+    scene = dict(trajectory=1, room=(8, 8, 3), n_spheres=20, n_boxes=12, radius=2.5, speed=0.5, fps=30, seed=2)
+    cfg = H.small_config(L, 1, voxel_size=0.005, truncation=0.02, num_buckets=1 << 21, num_blocks=1 << 20,
+                         w_rgb=0.1)
+    fr = H.frames(L, K, 5, step=12, **scene)
+    m = L.DenseMapping(K, cfg)
+    om = _oracle_map(L, cfg, K)
+    for d, c, T in fr:
+        dm = H.depth_m(d)
+        m.update(H.cuda(dm), H.cuda(c), T)
+        om.fuse(dm, c, T)
+        assert np.array_equal(H.sort_blocks(m.visible_blocks())[0], H.sort_blocks(om.visible())[0])
+    _compare_maps(m.export(), om.export(), exact=True)
+    assert m.stats().status == 0 and m.stats().allocated_blocks > 10000
+    T = fr[-1][2]
+    vm = torch.full((K.height, K.width, 4), float("nan"), device="cuda")
+    m.raycast(vm, T)
+    g, o = vm.cpu().numpy(), om.raycast(T)
+    assert np.array_equal(m.zrange(), om.zrange())
+    gh, oh = ~np.isnan(g[..., 2]), ~np.isnan(o[..., 2])
+    assert np.array_equal(gh, oh) and gh.mean() > 0.5  # surfaces beyond the 4 m fusion range stay empty
+    assert np.array_equal(g[gh], o[oh])
+    ov, _ = om.mesh(0, 1 << 23)
+    vtx = torch.zeros((len(ov) + 16, 3, 3), dtype=torch.float32, device="cuda")
+    n = m.fetch_mesh_vertex_only(vtx)
+    assert n == len(ov) and n > 100000
+    assert np.array_equal(H.sort_tris(vtx[:n].cpu().numpy())[0], H.sort_tris(ov)[0])
+
+    seq = H.frames(L, K, 10, **scene)
+    s = L.System(K, cfg)
+    s.set_pose(seq[0][2])
+    osys = O.OracleSystem(O.config_from(cfg), O.intrinsics_from(K), "f32")
+    osys.set_pose(seq[0][2])
+    # Both fail frame 1 by the reference's rule (the first tracked frame moves
+    # 16.7 mm toward the scene, beyond the 1 cm ICP gate, and the coarsest level
+    # finds no inlier: NaN error).  The two FP32 loops sum in different orders
+    # and then fuse at their own poses, so the poses part by a few tenths of a
+    # millimetre over the frames (measured 0.37 mm at frame 9, 0.73 at 18).
+    for k, (d, c, T) in enumerate(seq):
+        s.process_images(H.cuda(d), H.cuda(c))
+        osys.process(d, c)
+        assert np.abs(s.get_camera_pose()[:3, 3] - osys.pose()[:3, 3]).max() < 1e-3
+        assert s.stats().track.success == osys.last_result().success
