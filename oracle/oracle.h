@@ -91,6 +91,9 @@ typedef struct or_system_f64 or_system_f64;
     /* icp_reduce + rgb_step sums for pose T (row-major 3x4 floats) */                                             \
     void or_reduce_##S(const or_frame_##S *ref, const or_frame_##S *cur, int level, const float T[12],            \
                        float stddev, double out[58]);                                                              \
+    /* the same sums' terms per pixel, rounded to float: terms[p*58 + k] (0 without a correspondence) */          \
+    void or_reduce_terms_##S(const or_frame_##S *ref, const or_frame_##S *cur, int level, const float T[12],      \
+                             float stddev, float *terms);                                                          \
     /* DenseTracking::compute_transform */                                                                         \
     void or_track_##S(const or_frame_##S *ref, const or_frame_##S *cur, const double init[16],                    \
                       or_track_result *res);                                                                       \
@@ -117,6 +120,9 @@ int or_tri_table(int cube, int out[16]);   /* fills -1-terminated list, returns 
 /* renderScene / renderSceneTextured (cuda_imgproc.cu:17-108): float4 camera-frame
  * vertex / normal maps, rgb8 (NULL = untextured) -> rgba8 */
 void or_render_scene(const float *vmap, const float *nmap, const uint8_t *rgb, int w, int h, uint8_t *out);
+/* Column sums of an n x width float matrix, sequentially down each column in
+ * float: plain (kahan = 0) or compensated (Kahan 1965, kahan = 1). */
+void or_sum_f32(const float *terms, long long n, int width, int kahan, double *out);
 int or_edge_table(int cube);
 short or_pack_sdf(float v);
 float or_unpack_sdf(short v);

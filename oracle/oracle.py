@@ -77,6 +77,7 @@ def lib() -> C.CDLL:
                 f"or_frame_get_{s}": (None, [P, C.c_int, C.c_int, P]),
                 f"or_frame_set_vmap_{s}": (None, [P, P]),
                 f"or_reduce_{s}": (None, [P, P, C.c_int, C.POINTER(C.c_float), C.c_float, D]),
+                f"or_reduce_terms_{s}": (None, [P, P, C.c_int, C.POINTER(C.c_float), C.c_float, P]),
                 f"or_track_{s}": (None, [P, P, D, C.POINTER(OrTrackResult)]),
                 f"or_system_create_{s}": (P, [C.POINTER(OrConfig), C.POINTER(OrIntrinsics)]),
                 f"or_system_destroy_{s}": (None, [P]),
@@ -109,6 +110,8 @@ def lib() -> C.CDLL:
         L.or_unpack_sdf.argtypes = [C.c_short]
         L.or_render_scene.restype = None
         L.or_render_scene.argtypes = [P, P, P, C.c_int, C.c_int, P]
+        L.or_sum_f32.restype = None
+        L.or_sum_f32.argtypes = [P, C.c_longlong, C.c_int, C.c_int, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -258,6 +261,24 @@ def reduce(ref: OracleFrame, cur: OracleFrame, level: int, T, stddev: float = 0.
     Tf = (C.c_float * 12)(*np.asarray(T, np.float64).reshape(-1)[:12].astype(np.float32).tolist())
     out = (C.c_double * 58)()
     getattr(lib(), f"or_reduce_{ref.s}")(ref.h, cur.h, level, Tf, stddev, out)
+    return np.array(out[:])
+
+
+def reduce_terms(ref: OracleFrame, cur: OracleFrame, level: int, T, stddev: float = 0.0) -> np.ndarray:
+    """The float terms reduce() adds, per pixel: (pixels, 58)."""
+    Tf = (C.c_float * 12)(*np.asarray(T, np.float64).reshape(-1)[:12].astype(np.float32).tolist())
+    K = ref.K
+    w, h = K.width >> level, K.height >> level
+    out = np.zeros((w * h, 58), np.float32)
+    getattr(lib(), f"or_reduce_terms_{ref.s}")(ref.h, cur.h, level, Tf, stddev, _p(out))
+    return out
+
+
+def sum_f32(terms: np.ndarray, kahan: bool) -> np.ndarray:
+    """Sequential float column sums of terms, plain or Kahan-compensated."""
+    t = np.ascontiguousarray(terms, np.float32)
+    out = (C.c_double * t.shape[1])()
+    lib().or_sum_f32(_p(t), t.shape[0], t.shape[1], 1 if kahan else 0, out)
     return np.array(out[:])
 
 

@@ -128,3 +128,24 @@ void or_render_scene(const float *vmap, const float *nmap, const uint8_t *rgb, i
         render_point(p, n, img, light, out + 4 * i);
     }
 }
+
+/* Sequential float column sums, plain or with Kahan's compensation
+ * (W. Kahan, "Further remarks on reducing truncation errors", CACM 8(1), 1965):
+ * the yardsticks the GPU reduction's summation error is compared with. */
+void or_sum_f32(const float *terms, long long n, int width, int kahan, double *out) {
+    for (int k = 0; k < width; ++k) {
+        float s = 0.f, c = 0.f;
+        for (long long i = 0; i < n; ++i) {
+            const float x = terms[i * width + k];
+            if (kahan) {
+                const float y = x - c;
+                const float t = s + y;
+                c = (t - s) - y;
+                s = t;
+            } else {
+                s += x;
+            }
+        }
+        out[k] = (double)s;
+    }
+}

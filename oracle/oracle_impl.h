@@ -1059,6 +1059,30 @@ void SFX(or_reduce)(const FRAME *ref, const FRAME *cur, int l, const float Tf[12
     free(rows);
 }
 
+/* The terms or_reduce adds, per pixel: the 28 products of each row's upper
+ * triangle rounded to float, and 1 for the count (reduce_sum.h:48-61). */
+void SFX(or_reduce_terms)(const FRAME *ref, const FRAME *cur, int l, const float Tf[12], float stddev, float *terms) {
+    set_threads(ref->cfg.threads);
+    M34 T;
+    for (int i = 0; i < 12; ++i) T.m[i] = TO_R(Tf[i]);
+    const int n = ref->w[l] * ref->h[l];
+#pragma omp parallel for schedule(static)
+    for (int p = 0; p < n; ++p) {
+        float *t = terms + (size_t)p * 58;
+        for (int k = 0; k < 58; ++k) t[k] = 0.f;
+        R row[7];
+        for (int part = 0; part < 2; ++part) {
+            const int ok = part == 0 ? icp_row(ref, cur, l, &T, p, row) : rgb_row(ref, cur, l, &T, TO_R(stddev), p, row);
+            if (!ok) continue;
+            float *a = t + 29 * part;
+            int k = 0;
+            for (int i = 0; i < 7; ++i)
+                for (int j = i; j < 7; ++j) a[k++] = (float)(row[i] * row[j]);
+            a[28] = 1.f;
+        }
+    }
+}
+
 /* FP64 6x6 LDL^T with symmetric diagonal pivoting (documented Eigen::LDLT
  * method, icp_tracker.cpp:92); a zero pivot yields a zero component */
 static void ldlt6(double A[6][6], const double b[6], double x[6]) {
