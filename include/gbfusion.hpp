@@ -10,6 +10,8 @@
 //   fusion::DenseTracking    include/tracking/icp_tracker.h:28-88
 //   fusion::DenseOdometry    include/tracking/rgbd_odometry.h:13-41
 //   fusion::System           include/system.h:17-95
+// fusion::FusionBatch (no counterpart in the reference) serves many sessions
+// per launch: gbf_batch_* of gbfusion.h.
 // Errors raise fusion::Error (the reference prints and exits the process,
 // include/utils/safe_call.h:13-23).
 #ifndef GBFUSION_HPP
@@ -82,7 +84,14 @@ class Session {
         s_.reset(s, [](gbf_session *p) { gbf_session_destroy(p); });
     }
     gbf_session *handle() const { return s_.get(); }
+    std::shared_ptr<gbf_session> shared_handle() const { return s_; }
     const IntrinsicMatrix &intrinsics() const { return K_; }
+    // the next frame from host or device memory, into the session's own input
+    // buffers (for gbf_batch_process or gbf_process_frame_staged)
+    void stage(const void *depth_mm, int64_t depth_pitch, const void *rgb, int64_t rgb_pitch, void *stream = nullptr) {
+        check(gbf_session_stage(handle(), (const uint16_t *)depth_mm, depth_pitch, (const uint8_t *)rgb, rgb_pitch,
+                                stream), "Session::stage");
+    }
     const gbf_config &config() const { return cfg_; }
 
   protected:
@@ -177,6 +186,60 @@ class System : public DenseTracking {
         return p;
     }
     void set_pose(const Pose &p, void *stream = nullptr) { check(gbf_set_pose(handle(), p.data(), stream), "set_pose"); }
+};
+
+// Serving: the sessions in its slots advance one frame per tick, all in the
+// same launches (a captured graph per tick shape).  The batch keeps every
+// session it holds alive; it is destroyed (flushing what staggered groups owe)
+// before it lets them go.
+class FusionBatch {
+  public:
+    explicit FusionBatch(int max_sessions) : held_(max_sessions) {
+        gbf_batch *b = nullptr;
+        check(gbf_batch_create(max_sessions, &b), "gbf_batch_create");
+        b_.reset(b, [](gbf_batch *p) { gbf_batch_destroy(p); });
+    }
+    gbf_batch *handle() const { return b_.get(); }
+    // put a session into a slot (nullptr empties it)
+    void set(int slot, const Session *s) {
+        check(gbf_batch_set(handle(), slot, s ? s->handle() : nullptr), "FusionBatch::set");
+        held_.at(slot) = s ? s->shared_handle() : nullptr;
+    }
+    // frames read from device memory at each tick (nullptr, nullptr: the session's staging)
+    void set_inputs(int slot, const uint16_t *depth_dev, const uint8_t *rgb_dev) {
+        check(gbf_batch_set_inputs(handle(), slot, depth_dev, rgb_dev), "FusionBatch::set_inputs");
+    }
+    // copy the next tick's frame (host or device memory) on `stream`, overlapping the running tick
+    void stage(int slot, const void *depth_mm, int64_t depth_pitch, const void *rgb, int64_t rgb_pitch,
+               void *stream = nullptr) {
+        check(gbf_batch_stage(handle(), slot, (const uint16_t *)depth_mm, depth_pitch, (const uint8_t *)rgb,
+                              rgb_pitch, stream), "FusionBatch::stage");
+    }
+    void process(const std::vector<uint8_t> &active, bool use_graph = true, void *stream = nullptr) {
+        check(gbf_batch_process(handle(), active.data(), use_graph ? 1 : 0, stream), "FusionBatch::process");
+    }
+    // per-slot pose, tracking flag and status of the last tick (back = 0) or the one before
+    std::vector<gbf_slot_result> results(int back = 0) {
+        std::vector<gbf_slot_result> r(held_.size());
+        check(gbf_batch_results(handle(), back, r.data(), (int32_t)r.size()), "FusionBatch::results");
+        return r;
+    }
+    void set_groups(int groups) { check(gbf_batch_set_groups(handle(), groups), "FusionBatch::set_groups"); }
+    void set_stagger(bool on) { check(gbf_batch_set_stagger(handle(), on ? 1 : 0), "FusionBatch::set_stagger"); }
+    void set_ray_tile(int tile_w) { check(gbf_batch_set_ray_tile(handle(), tile_w), "FusionBatch::set_ray_tile"); }
+    void autotune(bool on = true, int ticks_per_candidate = 6) {
+        check(gbf_batch_set_autotune(handle(), on ? 1 : 0, ticks_per_candidate), "FusionBatch::autotune");
+    }
+    gbf_tuning tuning() const {
+        gbf_tuning t;
+        check(gbf_batch_tuning(handle(), &t), "FusionBatch::tuning");
+        return t;
+    }
+    void flush(void *stream = nullptr) { check(gbf_batch_flush(handle(), stream), "FusionBatch::flush"); }
+
+  private:
+    std::vector<std::shared_ptr<gbf_session>> held_;  // declared first: released after the batch
+    std::shared_ptr<gbf_batch> b_;
 };
 
 // DenseOdometry::trackFrame keeps the reference pyramid between frames; in this

@@ -43,3 +43,88 @@ def test_cpp_shim_compiles_and_runs(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     assert out[0] == "320" and out[1] == "240" and out[2] == "159.7500"
     assert int(out[3]) > 200000 * 512 * 10 and out[4] == "1"
+
+
+BATCH_SRC = r'''
+#include "gbfusion.hpp"
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <cstring>
+// Two sessions served by a tuned FusionBatch against a third processing the
+// same frames alone through System::process_images: bit-identical poses.
+int main() {
+    fusion::IntrinsicMatrix K(320, 240, 262.5f, 262.5f, 159.75f, 119.75f);
+    gbf_config c = fusion::default_config();
+    c.voxel_size = 0.01f; c.truncation = 0.03f; c.zmax_update = 4.f; c.zmax_raycast = 4.f;
+    c.num_levels = 3; c.max_iterations[0] = 10; c.max_iterations[1] = 5; c.max_iterations[2] = 3;
+    c.num_blocks = 1 << 15; c.num_buckets = 1 << 17; c.voxel_layout = GBF_VOXEL_SNORM;
+    gbf_synth_params sp;
+    fusion::check(gbf_synth_default(&sp), "synth_default");
+    gbf_synth_scene *sc = nullptr;
+    fusion::check(gbf_synth_create(&sp, &sc), "synth_create");
+    const int n = 24, W = K.width, H = K.height;
+    uint16_t *depth = nullptr;
+    uint8_t *rgb = nullptr;
+    if (cudaMalloc(&depth, (size_t)W * H * 2 * n) != cudaSuccess || cudaMalloc(&rgb, (size_t)W * H * 3 * n) != cudaSuccess)
+        return 2;
+    gbf_intrinsics k = K.c();
+    fusion::Pose T0;
+    fusion::check(gbf_synth_pose(sc, 0, T0.data()), "synth_pose");
+    for (int f = 0; f < n; ++f) {
+        fusion::Pose T;
+        fusion::check(gbf_synth_pose(sc, f, T.data()), "synth_pose");
+        fusion::check(gbf_synth_render(sc, &k, T.data(), f, depth + (size_t)f * W * H, rgb + (size_t)f * W * H * 3,
+                                       nullptr), "synth_render");
+    }
+    fusion::System a(K, c), b(K, c), alone(K, c);
+    a.set_pose(T0); b.set_pose(T0); alone.set_pose(T0);
+    fusion::FusionBatch batch(2);
+    batch.set(0, &a);
+    batch.set(1, &b);
+    batch.autotune(true, 2);
+    for (int f = 0; f < n; ++f) {
+        uint16_t *d = depth + (size_t)f * W * H;
+        uint8_t *r = rgb + (size_t)f * W * H * 3;
+        batch.stage(0, d, W * 2, r, W * 3);
+        batch.set_inputs(1, d, r);
+        batch.process({1, 1});
+        fusion::DeviceImageView dv{d, (int64_t)W * 2, H, W}, rv{r, (int64_t)W * 3, H, W};
+        alone.process_images(dv, rv);
+    }
+    std::vector<gbf_slot_result> res = batch.results(0);
+    batch.flush();
+    const fusion::Pose pa = a.get_camera_pose(), pb = b.get_camera_pose(), p1 = alone.get_camera_pose();
+    const bool same = memcmp(pa.data(), p1.data(), sizeof(pa)) == 0 && memcmp(pb.data(), p1.data(), sizeof(pb)) == 0 &&
+                      memcmp(res[0].pose, p1.data(), sizeof(pa)) == 0;
+    const gbf_tuning t = batch.tuning();
+    printf("%d %d %lld %d %d\n", same ? 1 : 0, res[1].tracked, (long long)res[1].frame_index, t.state, t.n_tried);
+    cudaFree(depth);
+    cudaFree(rgb);
+    gbf_synth_destroy(sc);
+    return 0;
+}
+'''
+
+
+@pytest.mark.gpu
+def test_cpp_batch_serves_like_single_sessions(tmp_path):
+    """FusionBatch from C++: a staged slot and a slot reading device frames,
+    under the launch-shape tuner, end with the pose of the same frames
+    processed alone."""
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no g++")
+    from libfusion_gb300 import build as B
+    lib = B.build()
+    src = tmp_path / "b.cpp"
+    src.write_text(BATCH_SRC)
+    exe = tmp_path / "b"
+    cuda = Path("/usr/local/cuda")
+    r = subprocess.run([gxx, "-std=c++17", "-I", str(ROOT / "include"), "-I", str(cuda / "include"), str(src), "-o",
+                        str(exe), str(lib), f"-Wl,-rpath,{lib.parent}", "-L", str(cuda / "lib64"), "-lcudart"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=300).stdout.split()
+    assert out[0] == "1", "batched and single-session poses differ"
+    assert out[1] == "1" and out[2] == "24"
+    assert int(out[3]) in (1, 2) and int(out[4]) >= 1  # the tuner explored (and may have settled)
