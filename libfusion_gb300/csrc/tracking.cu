@@ -28,72 +28,154 @@ namespace gbf {
 namespace {
 
 // ---------------------------------------------------------------------------
-// FP64 6x6 LDL^T with symmetric diagonal pivoting (the documented method of
-// Eigen::LDLT used at icp_tracker.cpp:92); zero pivots act as a pseudo-inverse.
-__device__ void ldlt_solve6(double A[6][6], const double b[6], double x[6]) {
-    int perm[6] = {0, 1, 2, 3, 4, 5};
-    double D[6];
+// The Gauss-Newton step in FP64, spread over one warp: the 6x6 LDL^T with
+// symmetric diagonal pivoting (the documented method of Eigen::LDLT used at
+// icp_tracker.cpp:92; zero pivots act as a pseudo-inverse), the SE(3)
+// exponential of xi = (rho, phi), translation first (Sophus convention), and
+// the pose composition.  A dependent FP64 operation takes about 70 cycles on
+// this part and a division about 600: one thread doing the step alone took
+// ~26 us (and spilled the pivoted matrix to local memory), one warp takes
+// ~12 us.  Each value sees the same operations in the same order as in the
+// one-thread form (row-by-row elimination, forward and back substitution,
+// W^2, I + A W + B W^2 and V), which 4,000 generated cases reproduced bit for
+// bit, zero pivots and ties in the pivot search included.
+
+// Full-warp shuffles: every lane must reach each call (none may sit inside a
+// lane-dependent branch or operand).
+__device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ int shfl_i(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+// lane holding the unordered pair {a, b} of a symmetric 6x6 matrix (lower triangle, 21 lanes)
+__device__ __forceinline__ int tri6(int a, int b) { return a >= b ? a * (a + 1) / 2 + b : b * (b + 1) / 2 + a; }
+__device__ __forceinline__ int diag6(int a) { return a * (a + 1) / 2 + a; }
+
+// x = A^-1 b.  In: lane tri6(r, c) holds A[r][c] (r >= c) in a,
+// lane o < 6 holds b[o] in bv.  Out: lane o < 6 gets x[o].  The symmetric
+// pivoting is a permutation the lanes track -- lane q < 6 holds perm[q] (the
+// original index at logical position q) and pos[q] (the logical position of
+// original index q) -- instead of moving rows and columns.
+__device__ double ldlt_solve6_warp(double a, double bv) {
+    const int lane = threadIdx.x & 31;
+    int r = 0;
+    while (r < 5 && (r + 1) * (r + 2) / 2 <= lane) ++r;
+    const int c = lane < 21 ? lane - r * (r + 1) / 2 : 0;
+    if (lane >= 21) r = 0;
+    int perm = lane, pos = lane;
+#pragma unroll
     for (int k = 0; k < 6; ++k) {
+        // the first logical i >= k with the largest |A(i,i)| (strictly larger replaces)
         int p = k;
-        double best = fabs(A[k][k]);
-        for (int i = k + 1; i < 6; ++i)
-            if (fabs(A[i][i]) > best) { best = fabs(A[i][i]); p = i; }
-        if (p != k) {
-            for (int j = 0; j < 6; ++j) { double t = A[k][j]; A[k][j] = A[p][j]; A[p][j] = t; }
-            for (int i = 0; i < 6; ++i) { double t = A[i][k]; A[i][k] = A[i][p]; A[i][p] = t; }
-            int t = perm[k]; perm[k] = perm[p]; perm[p] = t;
+        double best = fabs(shfl_d(a, diag6(shfl_i(perm, k))));
+#pragma unroll
+        for (int i = k + 1; i < 6; ++i) {
+            const double v = fabs(shfl_d(a, diag6(shfl_i(perm, i))));
+            if (v > best) {
+                best = v;
+                p = i;
+            }
         }
-        D[k] = A[k][k];
-        if (fabs(D[k]) <= DBL_MIN) {
-            for (int i = k + 1; i < 6; ++i) A[i][k] = 0.0;
+        if (p != k) {
+            const int ok = shfl_i(perm, k), op = shfl_i(perm, p);
+            if (lane == k) perm = op;
+            if (lane == p) perm = ok;
+            if (lane == ok) pos = p;
+            if (lane == op) pos = k;
+        }
+        const int pk = shfl_i(perm, k);
+        const double Dk = shfl_d(a, diag6(pk));
+        const int li = shfl_i(pos, r), lj = shfl_i(pos, c);
+        const int hi = max(li, lj), lo = min(li, lj);
+        const bool mine = lane < 21;
+        if (fabs(Dk) <= DBL_MIN) {
+            if (mine && lo == k && hi > k) a = 0.0;
             continue;
         }
-        for (int i = k + 1; i < 6; ++i) {
-            const double t = A[i][k];
-            A[i][k] = t / D[k];
-            for (int j = k + 1; j <= i; ++j) A[i][j] -= A[i][k] * A[j][k] * D[k];
-            // keep the upper triangle symmetric for the next pivot search / swaps
-            for (int j = k + 1; j <= i; ++j) A[j][i] = A[i][j];
-        }
+        if (mine && lo == k && hi > k) a = a / Dk;  // L(hi, k) = A(hi, k) / D(k)
+        const double Lh = shfl_d(a, tri6(shfl_i(perm, hi), pk));
+        const double Ll = shfl_d(a, tri6(shfl_i(perm, lo), pk));
+        if (mine && lo > k) a -= Lh * Ll * Dk;
     }
-    double z[6];
-    for (int i = 0; i < 6; ++i) z[i] = b[perm[i]];
-    for (int i = 0; i < 6; ++i)
-        for (int k = 0; k < i; ++k) z[i] -= A[i][k] * z[k];
-    for (int i = 0; i < 6; ++i) z[i] = (fabs(D[i]) > DBL_MIN) ? z[i] / D[i] : 0.0;
-    for (int i = 5; i >= 0; --i)
-        for (int k = i + 1; k < 6; ++k) z[i] -= A[k][i] * z[k];
-    for (int i = 0; i < 6; ++i) x[perm[i]] = z[i];
+    // forward: z[i] -= L(i, k) z[k], k ascending; lane q < 6 holds z[q] (logical)
+    const int src = lane < 6 ? perm : 0;
+    double z = shfl_d(bv, src);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const double zk = shfl_d(z, k);
+        const int pk = shfl_i(perm, k);  // every lane takes part in every shuffle
+        const double L = shfl_d(a, lane < 6 ? tri6(perm, pk) : 0);
+        if (lane > k && lane < 6) z -= L * zk;
+    }
+    {
+        const double Dq = shfl_d(a, lane < 6 ? diag6(perm) : 0);
+        if (lane < 6) z = (fabs(Dq) > DBL_MIN) ? z / Dq : 0.0;
+    }
+    // backward: z[i] -= L(k, i) z[k], k = i+1 .. 5 ascending
+#pragma unroll
+    for (int i = 4; i >= 0; --i) {
+        const int pi = shfl_i(perm, i);
+        double zi = shfl_d(z, i);
+#pragma unroll
+        for (int k = i + 1; k < 6; ++k) zi -= shfl_d(a, tri6(shfl_i(perm, k), pi)) * shfl_d(z, k);
+        if (lane == i) z = zi;
+    }
+    return shfl_d(z, lane < 6 ? pos : 0);  // x[perm[q]] = z[q]
 }
 
-// SE(3) exponential of xi = (rho, phi), translation first (Sophus convention).
-__device__ void se3_exp(const double xi[6], double T[12]) {
-    const double wx = xi[3], wy = xi[4], wz = xi[5];
+// element idx of W = [w]x (row-major 3x3)
+__device__ __forceinline__ double skew_at(int idx, double wx, double wy, double wz) {
+    return idx == 1 ? -wz : idx == 2 ? wy : idx == 3 ? wz : idx == 5 ? -wx : idx == 6 ? -wy : idx == 7 ? wx : 0.0;
+}
+
+// T = exp(xi) (lane o < 6 holds xi[o]); lane p < 12 gets T[p] (3x4 row-major).
+__device__ double se3_exp_warp(double xi) {
+    const int lane = threadIdx.x & 31;
+    const double x0 = shfl_d(xi, 0), x1 = shfl_d(xi, 1), x2 = shfl_d(xi, 2);
+    const double wx = shfl_d(xi, 3), wy = shfl_d(xi, 4), wz = shfl_d(xi, 5);
     const double th2 = wx * wx + wy * wy + wz * wz;
     const double th = sqrt(th2);
     double A, B, C;
     if (th < 1e-5) {
-        A = 1.0 - th2 / 6.0;
-        B = 0.5 - th2 / 24.0;
-        C = 1.0 / 6.0 - th2 / 120.0;
+        const double q = th2 / (lane == 0 ? 6.0 : lane == 1 ? 24.0 : 120.0);
+        A = 1.0 - shfl_d(q, 0);
+        B = 0.5 - shfl_d(q, 1);
+        C = 1.0 / 6.0 - shfl_d(q, 2);
     } else {
-        const double s = sin(th), c = cos(th);
-        A = s / th;
-        B = (1.0 - c) / th2;
-        C = (th - s) / (th2 * th);
+        double s, co;
+        sincos(th, &s, &co);  // the values of sin(th) and cos(th), one range reduction
+        // A = s / th, B = (1 - c) / th^2, C = (th - s) / (th^2 th): three lanes, one division
+        const double num = lane == 0 ? s : lane == 1 ? 1.0 - co : th - s;
+        const double den = lane == 0 ? th : lane == 1 ? th2 : th2 * th;
+        const double q = num / den;
+        A = shfl_d(q, 0);
+        B = shfl_d(q, 1);
+        C = shfl_d(q, 2);
     }
-    const double W[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
-    double W2[9];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) W2[i * 3 + j] = W[i * 3] * W[j] + W[i * 3 + 1] * W[3 + j] + W[i * 3 + 2] * W[6 + j];
-    double V[9];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            const double I = (i == j) ? 1.0 : 0.0;
-            T[i * 4 + j] = I + A * W[i * 3 + j] + B * W2[i * 3 + j];
-            V[i * 3 + j] = I + B * W[i * 3 + j] + C * W2[i * 3 + j];
-        }
-    for (int i = 0; i < 3; ++i) T[i * 4 + 3] = V[i * 3] * xi[0] + V[i * 3 + 1] * xi[1] + V[i * 3 + 2] * xi[2];
+    // lane e < 9: rotation and V element (i, j) = (e / 3, e % 3)
+    const int e = lane < 9 ? lane : 0, i = e / 3, j = e % 3;
+    const double w2 = skew_at(i * 3, wx, wy, wz) * skew_at(j, wx, wy, wz) +
+                      skew_at(i * 3 + 1, wx, wy, wz) * skew_at(3 + j, wx, wy, wz) +
+                      skew_at(i * 3 + 2, wx, wy, wz) * skew_at(6 + j, wx, wy, wz);
+    const double I = (i == j) ? 1.0 : 0.0, w = skew_at(e, wx, wy, wz);
+    const double rot = I + A * w + B * w2;
+    const double V = I + B * w + C * w2;
+    // lane i < 3: translation V[i] . (x0, x1, x2)
+    const int t = lane < 3 ? lane : 0;
+    const double tr = shfl_d(V, t * 3) * x0 + shfl_d(V, t * 3 + 1) * x1 + shfl_d(V, t * 3 + 2) * x2;
+    // pose layout: lane p = ri * 4 + rj
+    const int ri = lane < 12 ? lane / 4 : 0, rj = lane < 12 ? lane % 4 : 0;
+    const double rv = shfl_d(rot, ri * 3 + (rj < 3 ? rj : 0));
+    const double tv = shfl_d(tr, ri);
+    return rj == 3 ? tv : rv;
+}
+
+// c = a b (pose_mul) with a spread over the warp (lane p < 12 holds a[p]) and b in
+// memory; lane p < 12 gets c[p].
+__device__ double pose_mul_warp(double ap, const double *b) {
+    const int lane = threadIdx.x & 31;
+    const int i = lane < 12 ? lane / 4 : 0, j = lane < 12 ? lane % 4 : 0;
+    const double a0 = shfl_d(ap, i * 4), a1 = shfl_d(ap, i * 4 + 1), a2 = shfl_d(ap, i * 4 + 2);
+    const double a3 = shfl_d(ap, i * 4 + 3);
+    if (j < 3) return (a0 * b[0 * 4 + j] + a1 * b[1 * 4 + j]) + a2 * b[2 * 4 + j];
+    return ((a0 * b[3] + a1 * b[7]) + a2 * b[11]) + a3;
 }
 
 // |log(T)| of an SE(3) element (the success test, icp_tracker.cpp:145)
@@ -281,12 +363,22 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 // rows, warps 4-7 photometric rows (29 sums per thread), each thread 8 pixels
 // 128 apart; warp shuffle tree, then a fixed-order pass over the four warps of
 // each half.  Writes 58 floats to part.
-__device__ __forceinline__ void cta_partial(const SessionView &sv, int level, int rs, int cs, const M34 &T,
-                                            float stddev, int cta, int tile, float *part) {
-    __shared__ float warp_sums[kReduceThreads / 32][29];
-    __shared__ __align__(16) float4 s_v[kCtaPixels];
-    __shared__ __align__(16) float4 s_n[kCtaPixels];
-    __shared__ __align__(16) float s_i[kCtaPixels];
+// Shared memory of a reduction CTA.  The last CTA of a session reuses the
+// staging tile for the sum of the partial records (sum_partials), so the sum
+// costs no shared memory of its own: 8 KB more per CTA measured slower, L1
+// (which the projected gathers hit 55% of the time) giving way to it.
+struct ReduceSmem {
+    float warp_sums[kReduceThreads / 32][29];
+    __align__(16) float4 s_v[kCtaPixels];
+    __align__(16) float4 s_n[kCtaPixels];
+    __align__(16) float s_i[kCtaPixels];
+};
+
+__device__ __forceinline__ void cta_partial(ReduceSmem &sm, const SessionView &sv, int level, int rs, int cs,
+                                            const M34 &T, float stddev, int cta, int tile, float *part) {
+    auto &warp_sums = sm.warp_sums;
+    float4 *s_v = sm.s_v, *s_n = sm.s_n;
+    float *s_i = sm.s_i;
     const PhotoConst pc = photo_const(stddev);
     const int P = sv.lv[level].w * sv.lv[level].h;
     const int first = cta * tile;  // tile <= kCtaPixels, a multiple of 4 (16-byte aligned copies)
@@ -329,20 +421,62 @@ __device__ __forceinline__ void cta_partial(const SessionView &sv, int level, in
     }
 }
 
-// Sum of the n partial records in FP64: 4 groups of 64 threads take every
-// fourth record in order, then the 4 group sums are added in order.
-__device__ __forceinline__ void sum_partials(const float *parts, int n, double *total) {
-    __shared__ double grp[4][kPartialStride];
-    const int g = threadIdx.x >> 6, k = threadIdx.x & 63;
-    if (k < kReduceWidth) {
-        double s = 0.0;
-#pragma unroll 4
-        for (int c = g; c < n; c += 4) s += (double)__ldcg(parts + (size_t)c * kPartialStride + k);
-        grp[g][k] = s;
+// Compensated float accumulation: s + c carries the running sum, c the
+// rounding errors of the additions, each found exactly by the branch-free
+// TwoSum of Knuth (TAOCP vol. 2, 4.2.2) / Moller (1965).  Needs every
+// operation rounded as written (no contraction, no reassociation).
+struct FSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x;
+        const float bp = t - s;
+        c += (s - (t - bp)) + (x - bp);
+        s = t;
     }
+    __device__ __forceinline__ void add(const FSum &o) {
+        add(o.s);
+        c += o.c;
+    }
+};
+
+// Sum of the n partial records, in a fixed order, by compensated float
+// addition (a single CTA adding thousands of values in FP64 is bound by this
+// part's FP64 rate, ~12 us at 300 records): thread t reads the 16-byte chunk
+// t % 16 (columns 4(t % 16) .. +3) of records t / 16, t / 16 + 16, ..., then the
+// 16 record groups are combined in group order and widened to double.
+constexpr int kSumGroups = kReduceThreads / (kPartialStride / 4);  // 16
+static_assert(sizeof(float2) * kSumGroups * kPartialStride <= sizeof(float4) * kCtaPixels,
+              "the group sums fit in the staging tile");
+__device__ __forceinline__ void sum_partials(ReduceSmem &sm, const float *parts, int n, double *total) {
+    auto grp = reinterpret_cast<float2 (*)[kPartialStride]>(sm.s_v);  // the tile is dead by now
+    const int g = threadIdx.x / (kPartialStride / 4), q = threadIdx.x % (kPartialStride / 4);
+    FSum s0, s1, s2, s3;
+    const float4 *p4 = reinterpret_cast<const float4 *>(parts) + q;
+#pragma unroll 4
+    for (int c = g; c < n; c += kSumGroups) {
+        const float4 v = __ldcg(p4 + (size_t)c * (kPartialStride / 4));
+        s0.add(v.x);
+        s1.add(v.y);
+        s2.add(v.z);
+        s3.add(v.w);
+    }
+    grp[g][4 * q] = make_float2(s0.s, s0.c);
+    grp[g][4 * q + 1] = make_float2(s1.s, s1.c);
+    grp[g][4 * q + 2] = make_float2(s2.s, s2.c);
+    grp[g][4 * q + 3] = make_float2(s3.s, s3.c);
     __syncthreads();
-    if (threadIdx.x < kReduceWidth)
-        total[threadIdx.x] = ((grp[0][threadIdx.x] + grp[1][threadIdx.x]) + grp[2][threadIdx.x]) + grp[3][threadIdx.x];
+    if (threadIdx.x < kReduceWidth) {
+        FSum t;
+#pragma unroll
+        for (int h = 0; h < kSumGroups; ++h) {
+            const float2 v = grp[h][threadIdx.x];
+            FSum o;
+            o.s = v.x;
+            o.c = v.y;
+            t.add(o);
+        }
+        total[threadIdx.x] = (double)t.s + (double)t.c;
+    }
     __syncthreads();
 }
 
@@ -388,7 +522,8 @@ __global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const Sess
     }
     __syncthreads();
     const int rs = ts->idx, cs = 1 - ts->idx;
-    cta_partial(sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.red_tile[level],
+    __shared__ ReduceSmem sm;
+    cta_partial(sm, sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.red_tile[level],
                 sv.partials + (size_t)blockIdx.x * kPartialStride);
     __threadfence();
     __syncthreads();
@@ -398,44 +533,49 @@ __global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const Sess
     if (ticket != (unsigned)sv.red_ctas[level] - 1u) return;
     __threadfence();
     __shared__ double total[kReduceWidth];
-    sum_partials(sv.partials, sv.red_ctas[level], total);
+    sum_partials(sm, sv.partials, sv.red_ctas[level], total);
     if (threadIdx.x < kReduceWidth) ts->last_sums[threadIdx.x] = total[threadIdx.x];
-    if (threadIdx.x == 0) {
-        sv.ctr[C_TICKET] = 0;
-        if (!a.once) gn_epilogue(sv, level, a.iter, total);
-    }
+    if (threadIdx.x == 0) sv.ctr[C_TICKET] = 0;
+    if (!a.once && threadIdx.x < 32) gn_epilogue(sv, level, a.iter, total);  // one warp
 }
 
-// Host loop body of DenseTracking::compute_transform (icp_tracker.cpp:52-139).
+// Host loop body of DenseTracking::compute_transform (icp_tracker.cpp:52-139),
+// run by the 32 lanes of one warp: create_jtjjtr (reduce_sum.h:48-61) into the
+// float matrices, A = w_icp H_icp + w_rgb H_rgb and b likewise widened to
+// double, the LDL^T solve, T <- exp(xi) T; then lane 0 keeps the books.
 __device__ void gn_epilogue(const SessionView &sv, int level, int iter, const double *s) {
     TrackState *ts = sv.ts;
-    // create_jtjjtr (reduce_sum.h:48-61): float matrices from the sums
-    float Hi[6][6], Hr[6][6], bi[6], br[6];
-    int k = 0;
-    for (int i = 0; i < 6; ++i)
-        for (int j = i; j < 7; ++j, ++k) {
-            const float vi = (float)s[k], vr = (float)s[29 + k];
-            if (j == 6) {
-                bi[i] = vi; br[i] = vr;
-            } else {
-                Hi[i][j] = Hi[j][i] = vi;
-                Hr[i][j] = Hr[j][i] = vr;
-            }
+    const int lane = threadIdx.x & 31;
+    // lane tri6(r, c) (r >= c): A[r][c]; lane o < 6: b[o].  The packed index of
+    // (i, j), i <= j < 7, is 7 i - i (i - 1) / 2 + (j - i).
+    double a = 0.0, bv = 0.0;
+    {
+        int r = 0;
+        while (r < 5 && (r + 1) * (r + 2) / 2 <= lane) ++r;
+        const int c = lane - r * (r + 1) / 2;  // c <= r
+        if (lane < 21) {
+            const int k = 7 * c - c * (c - 1) / 2 + (r - c);
+            a = (double)(sv.w_icp * (float)s[k] + sv.w_rgb * (float)s[29 + k]);
         }
+        if (lane < 6) {
+            const int k = 7 * lane - lane * (lane - 1) / 2 + (6 - lane);
+            bv = (double)(sv.w_icp * (float)s[k] + sv.w_rgb * (float)s[29 + k]);
+        }
+    }
+    const double xi = ldlt_solve6_warp(a, bv);
+    const double E = se3_exp_warp(xi);
+    const double next = pose_mul_warp(E, ts->est);
+    const double old = lane < 12 ? ts->est[lane] : 0.0;
+    __syncwarp();
+    if (lane < 12) {
+        ts->est_prev[lane] = old;
+        ts->est[lane] = next;
+    }
+    __syncwarp();
+    if (lane != 0) return;
     const float r_icp = (float)s[27], n_icp = (float)s[28];
     const float r_rgb = (float)s[29 + 27], n_rgb = (float)s[29 + 28];
     const float stddev_next = sqrtf(r_rgb / (n_rgb - 6.0f));
-    double A[6][6], b[6], xi[6];
-    for (int i = 0; i < 6; ++i) {
-        for (int j = 0; j < 6; ++j) A[i][j] = (double)(sv.w_icp * Hi[i][j] + sv.w_rgb * Hr[i][j]);
-        b[i] = (double)(sv.w_icp * bi[i] + sv.w_rgb * br[i]);
-    }
-    ldlt_solve6(A, b, xi);
-    double E[12], next[12];
-    se3_exp(xi, E);
-    pose_mul(E, ts->est, next);
-    pose_copy(ts->est, ts->est_prev);
-    pose_copy(next, ts->est);
     ts->iterations += 1;
     ts->level_iters[level] += 1;
     ts->pixel_iterations += (long long)sv.lv[level].w * sv.lv[level].h;
@@ -654,7 +794,8 @@ __global__ void __launch_bounds__(kReduceThreads, 3) reduce_static_kernel(Sessio
 #pragma unroll
         for (int i = 0; i < 12; ++i) T.m[i] = a.pose[i];
     __syncthreads();
-    cta_partial(sv, 0, 0, 1, T, a.stddev, blockIdx.x, kCtaPixels, scratch + (size_t)blockIdx.x * kPartialStride);
+    __shared__ ReduceSmem sm;
+    cta_partial(sm, sv, 0, 0, 1, T, a.stddev, blockIdx.x, kCtaPixels, scratch + (size_t)blockIdx.x * kPartialStride);
     __threadfence();
     __syncthreads();
     __shared__ unsigned int ticket;
@@ -664,7 +805,7 @@ __global__ void __launch_bounds__(kReduceThreads, 3) reduce_static_kernel(Sessio
     if (ticket != (unsigned)nctas - 1u) return;
     __threadfence();
     __shared__ double total[kReduceWidth];
-    sum_partials(scratch, nctas, total);
+    sum_partials(sm, scratch, nctas, total);
     if (threadIdx.x < kReduceWidth) out[threadIdx.x] = total[threadIdx.x];
     if (threadIdx.x == 0) *tk = 0u;
 }
