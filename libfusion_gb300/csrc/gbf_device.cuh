@@ -135,7 +135,11 @@ __device__ __forceinline__ bool coord_ok(int x, int y, int z) {
 
 // Home slot: computeHash modulo the slot count; for a power-of-two count the
 // non-negative remainder is the low bits.
-__device__ __forceinline__ int home_slot(const SessionView &sv, int x, int y, int z) {
+// Lookups take any view with the SessionView field names they read (table,
+// cap, cap_mask, max_probe): the session itself, or a copy of those fields a
+// kernel keeps in registers.
+template <class SV>
+__device__ __forceinline__ int home_slot(const SV &sv, int x, int y, int z) {
     if (sv.cap_mask >= 0) {
         const unsigned ux = (unsigned)x * 73856093u, uy = (unsigned)y * 19349669u, uz = (unsigned)z * 83492791u;
         return (int)((ux ^ uy ^ uz) & (unsigned)sv.cap_mask);
@@ -144,7 +148,8 @@ __device__ __forceinline__ int home_slot(const SessionView &sv, int x, int y, in
 }
 
 // Read-only lookup: pool block id or -1.
-__device__ __forceinline__ int find_block(const SessionView &sv, int bx, int by, int bz) {
+template <class SV>
+__device__ __forceinline__ int find_block(const SV &sv, int bx, int by, int bz) {
     if (!coord_ok(bx, by, bz)) return -1;
     const unsigned long long key = pack_key(bx, by, bz);
     int slot = home_slot(sv, bx, by, bz);
