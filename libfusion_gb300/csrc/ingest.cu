@@ -37,7 +37,7 @@ __device__ __forceinline__ int set_index(const SessionView &sv, int sel) {
     return sel ? idx : 1 - idx;
 }
 
-__global__ void __launch_bounds__(kTileW *kTileH) ingest_l0_kernel(const SessionView *svs, IngestArgs a) {
+__global__ void __launch_bounds__(kTileW *kTileH) ingest_l0_kernel(const SessionView *__restrict__ svs, IngestArgs a) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     const int W = sv.lv[0].w, H = sv.lv[0].h;
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kTileW *kTileH) ingest_l0_kernel(const Session
     sv.inten[set_index(sv, a.set_sel)][0][p] = grey;
 }
 
-__global__ void pyr_down_kernel(const SessionView *svs, int set_sel, int level) {
+__global__ void pyr_down_kernel(const SessionView *__restrict__ svs, int set_sel, int level) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || level >= sv.levels) return;
     const int w = sv.lv[level].w, h = sv.lv[level].h;
@@ -164,7 +164,7 @@ __device__ __forceinline__ void fuse_weight(const SessionView &sv, int i, float4
     sv.fuse_px[i] = make_float2(ok ? dist : __int_as_float(0x7fffffff), w);
 }
 
-__global__ void __launch_bounds__(256, 8) level_maps_kernel(const SessionView *svs, int set_sel, int tiles_per_level0) {
+__global__ void __launch_bounds__(256, 8) level_maps_kernel(const SessionView *__restrict__ svs, int set_sel, int tiles_per_level0) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     // flatten the levels: level l owns ceil(P_l / blockDim) CTAs

@@ -28,14 +28,14 @@ namespace {
 constexpr int kAllocTile = 16;        // 16x16 pixels per CTA
 constexpr int kSetSize = 1024;        // shared-memory key set per CTA
 
-__global__ void fuse_begin_kernel(const SessionView *svs) {
+__global__ void fuse_begin_kernel(const SessionView *__restrict__ svs) {
     const SessionView &sv = svs[blockIdx.x];
     if (!sv.active || threadIdx.x != 0) return;
     sv.ctr[C_FRAME] += 1;
     sv.ctr[C_NVIS] = 0;
 }
 
-__global__ void fuse_import_kernel(const SessionView *svs, FuseImport in) {
+__global__ void fuse_import_kernel(const SessionView *__restrict__ svs, FuseImport in) {
     const SessionView &sv = svs[0];
     const int W = sv.lv[0].w, H = sv.lv[0].h;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kAllocTile *kAllocTile) alloc_kernel(const Ses
 // depth_fusion.cu:317-331, mode 0; update_map_weighted_kernel, :390-405, mode 2):
 // every voxel projecting to a pixel shares them, so they are computed once per
 // pixel.  Mode 1 (System frames) gets the same values from level_maps_kernel.
-__global__ void fuse_prep_kernel(const SessionView *svs, int mode) {
+__global__ void fuse_prep_kernel(const SessionView *__restrict__ svs, int mode) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     const int n = sv.lv[0].w * sv.lv[0].h;
@@ -192,7 +192,7 @@ __device__ __forceinline__ bool block_in_frustum(const SessionView &sv, const M3
     return false;
 }
 
-__global__ void vis_begin_kernel(const SessionView *svs) {
+__global__ void vis_begin_kernel(const SessionView *__restrict__ svs) {
     const SessionView &sv = svs[blockIdx.x];
     if (!sv.active || threadIdx.x != 0) return;
     sv.ctr[C_NVIS] = 0;
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256, 6) visible_kernel(const SessionView *svs)
 constexpr int kIntThreads = 128;  // threads per integration CTA (512 / kIntThreads voxels each), 16 CTAs per SM
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(kIntThreads, 16) integrate_kernel(const SessionView *svs, int mode) {
+__global__ void __launch_bounds__(kIntThreads, 16) integrate_kernel(const SessionView *__restrict__ svs, int mode) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || sv.layout != LAYOUT) return;
     __shared__ M34 Tcw_s;

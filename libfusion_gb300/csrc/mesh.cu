@@ -168,7 +168,7 @@ __device__ __forceinline__ int cube_of(const MeshSmem &sm, int li, float s[8], i
 }
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(kBlockVoxels) mesh_count_kernel(const SessionView *svs, int mode, int *counts) {
+__global__ void __launch_bounds__(kBlockVoxels) mesh_count_kernel(const SessionView *__restrict__ svs, int mode, int *counts) {
     const SessionView &sv = svs[0];
     const int n = min(sv.ctr[C_NUSED], sv.pool);
     __shared__ MeshSmem sm;
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(kBlockVoxels) mesh_count_kernel(const SessionV
 }
 
 // exclusive scan of counts[0..n) in place, total into C_MESH_TRIS (one CTA)
-__global__ void mesh_scan_kernel(const SessionView *svs, int *counts) {
+__global__ void mesh_scan_kernel(const SessionView *__restrict__ svs, int *counts) {
     const SessionView &sv = svs[0];
     const int n = min(sv.ctr[C_NUSED], sv.pool);
     __shared__ long long carry;
@@ -237,7 +237,7 @@ __global__ void mesh_scan_kernel(const SessionView *svs, int *counts) {
 }
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(kBlockVoxels) mesh_emit_kernel(const SessionView *svs, int mode, const int *offsets,
+__global__ void __launch_bounds__(kBlockVoxels) mesh_emit_kernel(const SessionView *__restrict__ svs, int mode, const int *offsets,
                                                                  float3 *vtx, void *attr, long long max_tris) {
     const SessionView &sv = svs[0];
     const int n = min(sv.ctr[C_NUSED], sv.pool);

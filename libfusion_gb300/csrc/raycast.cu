@@ -22,7 +22,7 @@ namespace gbf {
 
 namespace {
 
-__global__ void zr_init_kernel(const SessionView *svs) {
+__global__ void zr_init_kernel(const SessionView *__restrict__ svs) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     const int n = sv.zr_w * sv.zr_h;
@@ -33,7 +33,7 @@ __global__ void zr_init_kernel(const SessionView *svs) {
     if (blockIdx.x == 0 && threadIdx.x == 0) sv.ctr[C_RENDER] = 0;
 }
 
-__global__ void __launch_bounds__(256, 6) zrange_kernel(const SessionView *svs) {
+__global__ void __launch_bounds__(256, 6) zrange_kernel(const SessionView *__restrict__ svs) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     __shared__ M34 Tcw;
@@ -223,7 +223,7 @@ constexpr int kRayThreads = 64;
 constexpr int kMaxMarch = 1 << 16;  // safety bound; the march advances >= 1 voxel per step
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionView *svs, float4 *vmap_ext,
+__global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionView *__restrict__ svs, float4 *vmap_ext,
                                                                   long long vmap_pitch, int tw) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || sv.layout != LAYOUT) return;
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionV
 }
 
 // cv::cuda::resize(vmap, 0.5): 2x2 mean of every channel
-__global__ void vmap_down_kernel(const SessionView *svs, int level) {
+__global__ void vmap_down_kernel(const SessionView *__restrict__ svs, int level) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || level >= sv.levels) return;
     const int w = sv.lv[level].w, h = sv.lv[level].h, pw = sv.lv[level - 1].w;
@@ -316,7 +316,7 @@ __global__ void vmap_down_kernel(const SessionView *svs, int level) {
 }
 
 // computeNMapK (cuda_imgproc.cu:276-294) over every level of the reference set
-__global__ void nmap_all_kernel(const SessionView *svs) {
+__global__ void nmap_all_kernel(const SessionView *__restrict__ svs) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
     int b = blockIdx.x, level = 0;

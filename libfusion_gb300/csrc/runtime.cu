@@ -142,7 +142,7 @@ __global__ void reset_table_kernel(HashSlot *t, int cap) {
 
 // canonical export of blocks [first, first+count): coords, float sdf/weight, rgb
 template <int LAYOUT>
-__global__ void export_kernel(const SessionView *svs, int first, int count, int *coords, float *sdf, float *w,
+__global__ void export_kernel(const SessionView *__restrict__ svs, int first, int count, int *coords, float *sdf, float *w,
                               unsigned char *rgb) {
     const SessionView &sv = svs[0];
     for (int b = blockIdx.x; b < count; b += gridDim.x) {
@@ -166,7 +166,7 @@ __global__ void export_kernel(const SessionView *svs, int first, int count, int 
 }
 
 template <int LAYOUT>
-__global__ void import_kernel(const SessionView *svs, int count, const int *coords, const float *sdf, const float *w,
+__global__ void import_kernel(const SessionView *__restrict__ svs, int count, const int *coords, const float *sdf, const float *w,
                               const unsigned char *rgb) {
     const SessionView &sv = svs[0];
     __shared__ int id_s;

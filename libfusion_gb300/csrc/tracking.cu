@@ -503,7 +503,7 @@ __device__ __forceinline__ bool session_runs(const SessionView &sv, const Reduce
 // tile adds the partials in a fixed order and takes the Gauss-Newton step.
 // Sessions that have left the level, or do not track this frame, return at
 // once.
-__global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const SessionView *svs, ReduceArgs a) {
+__global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const SessionView *__restrict__ svs, ReduceArgs a) {
     const SessionView &sv = svs[blockIdx.y];
     const int level = a.level;
     if (!session_runs(sv, a) || blockIdx.x >= sv.red_ctas[level]) return;
@@ -631,7 +631,7 @@ __device__ void gn_epilogue(const SessionView &sv, int level, int iter, const do
 }
 
 // frame_mode 1: System frame (track only when a reference exists); 0: gbf_track.
-__global__ void track_begin_kernel(const SessionView *svs, int frame_mode) {
+__global__ void track_begin_kernel(const SessionView *__restrict__ svs, int frame_mode) {
     const SessionView &sv = svs[blockIdx.x];
     if (!sv.active || threadIdx.x != 0) return;
     TrackState *ts = sv.ts;
@@ -653,7 +653,7 @@ __global__ void track_begin_kernel(const SessionView *svs, int frame_mode) {
 // Tracking result (icp_tracker.cpp:143-155); frame_mode 1 also applies the
 // System / DenseOdometry bookkeeping (rgbd_odometry.cpp:39-41): pose update
 // and reference swap.
-__global__ void track_finish_kernel(const SessionView *svs, int frame_mode) {
+__global__ void track_finish_kernel(const SessionView *__restrict__ svs, int frame_mode) {
     const SessionView &sv = svs[blockIdx.x];
     if (!sv.active || threadIdx.x != 0) return;
     TrackState *ts = sv.ts;
@@ -737,7 +737,7 @@ void launch_frame_finish(const SessionView *d_sv, int nslots, cudaStream_t st) {
 }
 
 namespace {
-__global__ void slot_results_kernel(const SessionView *svs, int n, gbf_slot_result *out) {
+__global__ void slot_results_kernel(const SessionView *__restrict__ svs, int n, gbf_slot_result *out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const SessionView &sv = svs[i];
