@@ -207,7 +207,7 @@ class ClockSampler:
 # DRAM bytes one pixel-iteration of the ICP + photometric reduction moves, from
 # one ncu capture of a level-0 launch over 4 sessions (100.83 MB for 1,228,800
 # pixel-iterations; profiles/gn_reduce_kernel_4x640x480.md): the roofline's traffic
-REDUCE_DRAM_BYTES_PER_PIXEL_ITER = 100.828160e6 / 1228800
+REDUCE_DRAM_BYTES_PER_PIXEL_ITER = 100.36224e6 / 1228800
 
 
 def measured_peaks():
@@ -539,7 +539,7 @@ def run_ours(args):
                 "launches_per_step": n_launch, "peak_source": f"{peak_kind} hbm_gbs",
                 "algorithmic_bytes_per_launch": bytes_step / n_launch, "algorithmic_bytes_per_step": bytes_step,
                 "traffic_basis": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0 launch at 4 "
-                                 "sessions (profiles/gn_reduce_kernel_4x640x480.md): 82.05 B per pixel-iteration, "
+                                 "sessions (profiles/gn_reduce_kernel_4x640x480.md): 81.7 B per pixel-iteration, "
                                  "times this run's pixel-iterations per launch" if traffic is not None else None,
                 "work_per_step": {"pixel_iterations": pix_iter, "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
                 "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream"}
