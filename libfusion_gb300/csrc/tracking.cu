@@ -8,9 +8,10 @@
 // two kernels, each re-reading the reference vertex map) into 29 + 29 FP32
 // sums (warp shuffle tree, then a fixed-order shared-memory pass), writes one
 // partial record, and the last CTA of the session (atomic ticket) adds the
-// partials in FP64 in CTA order and runs the step on the device: FP64 LDL^T
-// solve of the 6x6 system, SE(3) exponential, pose composition, and the
-// reference's error-increase / revert / break rules.  No host round trip: the
+// partials in a fixed order by compensated float addition, then its first warp
+// runs the step on the device: FP64 LDL^T solve of the 6x6 system, SE(3)
+// exponential, pose composition, and the reference's error-increase / revert /
+// break rules.  No host round trip: the
 // reference pays two device->host syncs per iteration (pose_estimator.cu:302-304,
 // m_estimator.cu:477-479).  The order of every sum is fixed, so a session's
 // result does not depend on the other sessions in the batch.
@@ -305,9 +306,9 @@ __device__ __forceinline__ bool rgb_row(const SessionView &sv, int level, int cs
 // The 28 products of the row's upper triangle added into the running sums, one
 // fused multiply-add each (the sums are a reduction compared within a
 // tolerance, not bit for bit; the rows themselves keep the reference's rounding).
-// A thread adds at most 8 pixels before the warp tree and the FP64 pass over
-// the CTAs: the summation error stays at or below that of a Kahan-compensated
-// sequential float sum without its 29 compensation registers.
+// A thread adds at most 8 pixels before the warp tree and the compensated pass
+// over the CTAs: the summation error stays at or below that of a
+// Kahan-compensated sequential float sum without its 29 compensation registers.
 __device__ __forceinline__ void accumulate(float *acc, const float row[7]) {
     int k = 0;
 #pragma unroll
