@@ -107,17 +107,17 @@ def tune_launch_shape(L, K, S, frames, poses0, per_candidate):
     return t
 
 
-def launch_shape(batch, args):
-    if args.no_autotune:
+def launch_shape(batch, args, tuned):
+    if tuned is None:
         batch.set_groups(args.groups)
     else:
         batch.autotune(True, args.tune_ticks)
 
 
-def shape_report(batch, tuned, args):
+def shape_report(batch, tuned, args, unsettled=None):
     t = batch.tuning()
     if tuned is None:
-        return {"autotune": False, **t["chosen"]}
+        return {"autotune": False, **t["chosen"], **({"note": unsettled} if unsettled else {})}
     return {"autotune": True, "settled_from_table": t["from_table"], "groups": t["chosen"]["groups"],
             "stagger": t["chosen"]["stagger"], "ray_tile_w": t["chosen"]["ray_tile_w"],
             "tuning_ticks": tuned["ticks"], "ticks_per_candidate": tuned["ticks_per_candidate"],
@@ -265,7 +265,8 @@ def aggregate_rate(sessions_per_rank: int, world: int, steps: int, total_ms: flo
 
 # ----------------------------------------------------------------------------- CPU
 
-def cpu_mix(L, K, warmup: int, steps: int, seconds: float | None = None, threads: int | None = None):
+def cpu_mix(L, K, warmup: int, steps: int, seconds: float | None = None, threads: int | None = None,
+            precision: str = "f32"):
     """The FP32 oracle (the reference's kernel bodies restated in C, OpenMP over
     pixels and blocks) on this machine's host cores: one CPU session per voxel
     size of the served mix, `warmup` untimed frames each, then frames timed
@@ -280,7 +281,7 @@ def cpu_mix(L, K, warmup: int, steps: int, seconds: float | None = None, threads
     mix = []
     for i in range(n_mix):
         fr = host_frames(L, K, per, seed=i)
-        sysm = O.OracleSystem(O.config_from(session_config(L, i), threads=threads), O.intrinsics_from(K), "f32")
+        sysm = O.OracleSystem(O.config_from(session_config(L, i), threads=threads), O.intrinsics_from(K), precision)
         sysm.set_pose(fr[0][2])
         for k in range(warmup):
             sysm.process(fr[k][0], fr[k][1])
@@ -321,14 +322,19 @@ def cpu_model() -> str:
 
 
 def cpu_baseline(L, K, seconds: float, warmup: int):
-    """All host threads on the bounded sample, and one thread on a third of it."""
+    """All host threads on the bounded sample, one thread on a third of it, and
+    the FP64 oracle (the error reference, not a baseline) on all threads."""
     t, n_mix, threads = cpu_mix(L, K, warmup, 256, seconds)
     t1, _, _ = cpu_mix(L, K, min(warmup, 2), 256, seconds / 3, threads=1)
+    t64, _, _ = cpu_mix(L, K, min(warmup, 2), 256, seconds / 3, precision="f64")
     return {"value": len(t) / sum(t), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": cpu_sample_text(len(t), n_mix, threads) + f", {sum(t):.1f} s",
             "cpu": cpu_model(), "nproc": os.cpu_count(),
             "single_thread": {"value": len(t1) / sum(t1), "unit": UNIT, "cores": 1,
-                              "sample": cpu_sample_text(len(t1), n_mix, 1) + f", {sum(t1):.1f} s"}}
+                              "sample": cpu_sample_text(len(t1), n_mix, 1) + f", {sum(t1):.1f} s"},
+            "fp64_oracle": {"value": len(t64) / sum(t64), "unit": UNIT, "cores": threads,
+                            "sample": cpu_sample_text(len(t64), n_mix, threads).replace("FP32", "FP64")
+                            + f", {sum(t64):.1f} s; the error reference, timed for the record"}}
 
 
 def host_frames(L, K, n, seed=0):
@@ -452,6 +458,9 @@ def run_ours(args):
     n_phase = min(steps, 8)
     n_serve = args.serve_ticks
     nfr = warm + steps + n_phase + n_serve
+    # the tuner's search: 10 candidates, each timed for --tune-ticks ticks after
+    # one untimed tick, plus the two ticks in flight at every switch
+    n_tune = 0 if args.no_autotune else 10 * (args.tune_ticks + 3) + 10
 
     # admission: every session's device bytes under a 150 GB budget per GPU
     budget = 150 * (1 << 30)
@@ -459,8 +468,12 @@ def run_ours(args):
     if need > budget:
         raise SystemExit(f"{S} sessions need {need/2**30:.1f} GiB > 150 GiB budget")
 
-    frames, poses0 = render_frames(L, K, replica_seeds(rank, S), nfr)
+    frames, poses0 = render_frames(L, K, replica_seeds(rank, S), max(nfr, n_tune))
     tuned = None if args.no_autotune else tune_launch_shape(L, K, S, frames, poses0, args.tune_ticks)
+    unsettled = None
+    if tuned is not None and tuned["state"] != "settled":  # fall back to the fixed shape
+        unsettled = f"the launch-shape search did not settle in {tuned['ticks']} ticks; --groups {args.groups} used"
+        tuned = None
     sessions = []
     for i in range(S):
         s = L.System(K, session_config(L, i))
@@ -469,7 +482,7 @@ def run_ours(args):
     batch = L.FusionBatch(S)
     for i, s in enumerate(sessions):
         batch.set(i, s)
-    launch_shape(batch, args)
+    launch_shape(batch, args, tuned)
     active = [True] * S
     use_graph = not args.no_graph
     stream = torch.cuda.Stream()
@@ -558,7 +571,7 @@ def run_ours(args):
     eb = L.FusionBatch(S)
     for i, s in enumerate(e2e_sessions):
         eb.set(i, s)
-    launch_shape(eb, args)
+    launch_shape(eb, args, tuned)
     copy = torch.cuda.Stream()
     got = []
 
@@ -640,7 +653,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warm,
         "ms_per_step": total_ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": dict(workload_config(S), graph=use_graph, launch_shape=shape_report(batch, tuned, args),
+        "config": dict(workload_config(S), graph=use_graph, launch_shape=shape_report(batch, tuned, args, unsettled),
                        l2="working set per tick (voxel pools, 64 x 640x480 pyramids) far above the 129 MB L2; no flush",
                        inputs="seeded synthetic RGB-D (sphere-traced SDF room, depth noise model) resident in HBM"),
         "latency_ms": {"p50": p(0.50), "p95": p(0.95), "p99": p(0.99), "basis": "tick duration (every session's "
