@@ -555,7 +555,12 @@ def run_ours(args):
                                  "sessions (profiles/gn_reduce_kernel_4x640x480.md): 81.7 B per pixel-iteration, "
                                  "times this run's pixel-iterations per launch" if traffic is not None else None,
                 "work_per_step": {"pixel_iterations": pix_iter, "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
-                "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream"}
+                "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream",
+                "why_this_kernel": "the raycast's march (the other ~35% of launch time, profiles/"
+                                   "launches_fusion_tick_64x640x480.md) is bound by instruction issue, not HBM "
+                                   "(76% issue active, DRAM 2.7%: profiles/raycast_kernel_4x640x480.md); the "
+                                   "HBM roofline is given for the larger memory-bound phase",
+                "march_ms_per_step": phases["march"] / 1.0}
 
     # ---- end to end through the public API with host buffers (pinned): the same
     # frames as the timed ticks, after the same warm-up frames (untimed).  Each
