@@ -560,7 +560,7 @@ def run_ours(args):
                                    "launches_fusion_tick_64x640x480.md) is bound by instruction issue, not HBM "
                                    "(76% issue active, DRAM 2.7%: profiles/raycast_kernel_4x640x480.md); the "
                                    "HBM roofline is given for the larger memory-bound phase",
-                "march_ms_per_step": phases["march"] / 1.0}
+                "march_ms_per_step": phases["march"]}
 
     # ---- end to end through the public API with host buffers (pinned): the same
     # frames as the timed ticks, after the same warm-up frames (untimed).  Each
