@@ -1153,7 +1153,8 @@ void tune_store(const gbf_batch *b, const gbf_batch::Shape &c) {
             e.second = c;
             return;
         }
-    g_tune_table.emplace_back(k, c);
+    const std::pair<TuneKey, gbf_batch::Shape> entry(k, c);
+    g_tune_table.push_back(entry);
 }
 
 float median_ms(std::vector<float> v) {
