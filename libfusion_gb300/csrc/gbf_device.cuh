@@ -176,7 +176,19 @@ struct Vox {
     uchar4 rgb;
 };
 
-__device__ __forceinline__ float sdf_ref_unpack(short v) { return (float)v / 32767.f; }
+// v / 32767.f correctly rounded (Voxel::getSDF, voxel.h:36-39) without a
+// division: q = v * RN(1/32767), then one correction with the exact residual
+// v - q * 32767 (Markstein's method; P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990).  Equal to the division for all 65,535 int16 codes (checked with exact
+// rational arithmetic, tests/test_arith_proofs.py).
+constexpr float kRefUnitRN = 1.0f / 32767.0f;  // RN(1/32767), evaluated at compile time
+__device__ __forceinline__ float sdf_ref_unpack(short v) {
+    const float x = (float)v;
+    const float q = x * kRefUnitRN;
+    const float e = __fmaf_rn(-q, 32767.f, x);
+    return __fmaf_rn(e, kRefUnitRN, q);
+}
 __device__ __forceinline__ short sdf_ref_pack(float v) { return (short)__float2int_rz(v * 32767.f); }
 __device__ __forceinline__ float weight_ref_store(float w) { return w > 255.f ? 255.f : w; }
 // HALF weight: the clamped float weight rounded to binary16 (11-bit significand,
