@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--serve-ticks", type=int, default=120, help="ticks of the churn (arrival / eviction) run")
     ap.add_argument("--layout", default="half", choices=sorted(LAYOUTS), help="voxel storage of every session")
+    ap.add_argument("--workload", default="served", choices=["served", "mixed"],
+                    help="mixed: sessions of three resolutions and three voxel sizes in one batch "
+                         "(served vs plain only; prints its own line)")
     return ap.parse_args()
 
 
@@ -80,13 +83,14 @@ def workload_config(sessions: int) -> dict:
             "hash_slots": 1 << 19, "pyramid": "3 levels 10/5/3"}
 
 
-def tune_launch_shape(L, K, S, frames, poses0, per_candidate):
+def tune_launch_shape(L, K, S, frames, poses0, per_candidate, make=None):
     """The batch tuner's search for this workload's shape, run on throwaway
     sessions of the same configurations over the first frames, so that the
-    measured batches settle from the process-wide table at their first tick."""
+    measured batches settle from the process-wide table at their first tick.
+    make(i) builds session i (default: the served workload's)."""
     import torch
     L.autotune_forget()
-    ss = [L.System(K, session_config(L, i)) for i in range(S)]
+    ss = [make(i) if make else L.System(K, session_config(L, i)) for i in range(S)]
     for i, s in enumerate(ss):
         s.set_pose(poses0[i])
     b = L.FusionBatch(S)
@@ -675,12 +679,118 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# the mixed workload: resolutions and voxel sizes cycled over the sessions
+MIXED_SIZES = ((320, 240), (640, 480), (1280, 720))
+MIXED_VOXELS = (0.004, 0.008, 0.016)
+
+
+def mixed_session(L, i):
+    """(intrinsics, config) of session i of the mixed workload."""
+    w, h = MIXED_SIZES[i % len(MIXED_SIZES)]
+    v = MIXED_VOXELS[(i // len(MIXED_SIZES)) % len(MIXED_VOXELS)]
+    s = w / 640.0
+    K = L.IntrinsicMatrix(w, h, 525.0 * s, 525.0 * s, (w - 1) / 2.0, (h - 1) / 2.0)
+    cfg = L.default_config(voxel_size=v, truncation=min(max(3.0 * v, 0.02), 0.05), zmin_update=0.3,
+                           zmax_update=4.0, zmin_raycast=0.3, zmax_raycast=4.0, num_buckets=1 << 19,
+                           num_blocks=1 << 18, voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3,
+                           max_iterations=[10, 5, 3, 3, 3], max_probe=256)
+    return K, cfg
+
+
+def run_mixed(args):
+    """Sessions of 320x240, 640x480 and 1280x720 with 4, 8 and 16 mm voxels in
+    one batch (every launch sized for the largest), against the same sessions
+    one at a time.  Frames per second count frames of every size alike."""
+    import torch
+    import libfusion_gb300 as L
+    from libfusion_gb300 import build as B
+    B.build()
+    S, steps, warm = args.sessions, args.steps, args.warmup
+    spec = [mixed_session(L, i) for i in range(S)]
+    n_tune = 0 if args.no_autotune else 10 * (args.tune_ticks + 3) + 10
+    nfr = max(warm + steps, n_tune)
+    frames, poses0 = [], []
+    for i, (K, _) in enumerate(spec):
+        sc = L.SynthScene(seed=1000 + i)
+        d = torch.empty((nfr, K.height, K.width), dtype=torch.uint16, device="cuda")
+        c = torch.empty((nfr, K.height, K.width, 3), dtype=torch.uint8, device="cuda")
+        for k in range(nfr):
+            sc.render_into(K, k, d[k].data_ptr(), c[k].data_ptr())
+        frames.append((d, c))
+        poses0.append(sc.pose(0))
+        sc.close()
+    torch.cuda.synchronize()
+    make = lambda i: L.System(*spec[i])
+    tuned = None if args.no_autotune else tune_launch_shape(L, None, S, frames, poses0, args.tune_ticks, make)
+    if tuned is not None and tuned["state"] != "settled":
+        tuned = None
+    sessions = [make(i) for i in range(S)]
+    for s, p in zip(sessions, poses0):
+        s.set_pose(p)
+    batch = L.FusionBatch(S)
+    for i, s in enumerate(sessions):
+        batch.set(i, s)
+    launch_shape(batch, args, tuned)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    active = [True] * S
+
+    def tick(k):
+        for i in range(S):
+            batch.set_inputs(i, frames[i][0][k].data_ptr(), frames[i][1][k].data_ptr())
+        batch.process(active)
+
+    for k in range(warm):
+        tick(k)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        ev[k][0].record(stream)
+        tick(warm + k)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    tick_ms = sorted(a.elapsed_time(b) for a, b in ev)
+    total_ms = ev[0][0].elapsed_time(ev[-1][1])
+    value = S * steps / (total_ms / 1e3)
+    shape = shape_report(batch, tuned, args)
+    batch.close()
+    del sessions
+    # the same sessions one at a time, one frame at a time, pose read back per frame
+    plain_s = [make(i) for i in range(S)]
+    for s, p in zip(plain_s, poses0):
+        s.set_pose(p)
+    for k in range(warm):
+        for i, s in enumerate(plain_s):
+            s.process_images(frames[i][0][k], frames[i][1][k])
+    torch.cuda.synchronize()
+    per = min(steps, args.plain_frames or steps)
+    t0 = time.perf_counter()
+    for k in range(per):
+        for i, s in enumerate(plain_s):
+            s.process_images(frames[i][0][warm + k], frames[i][1][warm + k])
+            s.get_pose()
+    torch.cuda.synchronize()
+    plain = S * per / (time.perf_counter() - t0)
+    p = lambda q: tick_ms[min(len(tick_ms) - 1, int(math.ceil(q * len(tick_ms))) - 1)]
+    print(json.dumps({
+        "metric": METRIC, "workload": "mixed", "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": warm, "ms_per_step": total_ms / steps, "higher_is_better": True,
+        "config": {"workload": f"{S} sessions per tick: resolutions {['%dx%d' % s for s in MIXED_SIZES]} and voxels "
+                               f"{[f'{v * 1000:.0f} mm' for v in MIXED_VOXELS]} cycled over the sessions",
+                   "voxel_layout": LAYOUTS[LAYOUT][1], "launch_shape": shape},
+        "latency_ms": {"p50": p(0.5), "p99": p(0.99)},
+        "plain": {"value": plain, "unit": UNIT, "frames": S * per}, "served_vs_plain": value / plain,
+    }), flush=True)
+
+
 def main():
     global LAYOUT
     args = parse()
     LAYOUT = args.layout
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "mixed":
+        run_mixed(args)
     else:
         run_ours(args)
 
