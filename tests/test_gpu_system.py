@@ -49,47 +49,58 @@ def test_system_matches_oracle_and_ground_truth(gbf):
 
 def test_batch_session_isolation(gbf):
     """A session gives the same result alone and batched with others of other
-    resolutions / voxel sizes (bit-identical pose and map)."""
+    resolutions / voxel sizes / voxel layouts (bit-identical pose and map)."""
     import torch
     L = gbf
     KA = H.intrinsics(L, 320, 240)
     KB = H.intrinsics(L, 160, 120)
+    KC = H.intrinsics(L, 256, 192)
     cfgA = H.small_config(L, 0)
     cfgB = H.small_config(L, 1, voxel_size=0.016, truncation=0.048)
+    cfgC = H.small_config(L, 2, voxel_size=0.008, truncation=0.03)
     frA = H.frames(L, KA, 5, seed=3)
     frB = H.frames(L, KB, 5, seed=9)
+    frC = H.frames(L, KC, 5, seed=11)
 
-    alone = L.System(KA, cfgA)
-    alone.set_pose(frA[0][2])
-    for d, c, T in frA:
-        alone.process_images(H.cuda(d), H.cuda(c))
-    pa = alone.get_camera_pose()
-    ma = alone.export()
+    def run_alone(K, cfg, fr):
+        s = L.System(K, cfg)
+        s.set_pose(fr[0][2])
+        for d, c, T in fr:
+            s.process_images(H.cuda(d), H.cuda(c))
+        return s.get_camera_pose(), s.export()
+
+    pa, ma = run_alone(KA, cfgA, frA)
+    pc, mc = run_alone(KC, cfgC, frC)
 
     for use_graph, groups in ((False, 1), (True, 1), (False, 2), (True, 3)):
         a = L.System(KA, cfgA)
         b = L.System(KB, cfgB)
         b2 = L.System(KB, cfgB)
+        cc = L.System(KC, cfgC)
         a.set_pose(frA[0][2])
         b.set_pose(frB[0][2])
         b2.set_pose(frB[0][2])
-        batch = L.FusionBatch(4)
+        cc.set_pose(frC[0][2])
+        batch = L.FusionBatch(5)
         batch.set(0, b)
+        batch.set(1, cc)
         batch.set(2, a)
         batch.set(3, b2)
         batch.set_groups(groups)
         for i in range(5):
-            for sess, (d, c, T) in ((a, frA[i]), (b, frB[i]), (b2, frB[i])):
+            for sess, (d, c, T) in ((a, frA[i]), (b, frB[i]), (b2, frB[i]), (cc, frC[i])):
                 sess.stage(H.cuda(d), H.cuda(c))
-            batch.process([True, True, True, True], use_graph=use_graph)
+            batch.process([True, True, True, True, True], use_graph=use_graph)
             torch.cuda.synchronize()
         assert np.array_equal(a.get_camera_pose(), pa)
+        assert np.array_equal(cc.get_camera_pose(), pc)
         batch.flush()  # the staggered group's last frame is fused here
-        mb = a.export()
-        for x, y in zip(ma, mb):
-            xs = H.sort_blocks(ma[0], x)[1]
-            ys = H.sort_blocks(mb[0], y)[1]
-            assert np.array_equal(xs, ys)
+        for alone_map, sess in ((ma, a), (mc, cc)):
+            mb = sess.export()
+            for x, y in zip(alone_map, mb):
+                xs = H.sort_blocks(alone_map[0], x)[1]
+                ys = H.sort_blocks(mb[0], y)[1]
+                assert np.array_equal(xs, ys)
         # the two identical B sessions agree with each other
         assert np.array_equal(b.get_camera_pose(), b2.get_camera_pose())
         batch.close()
