@@ -100,3 +100,21 @@ def test_invalid_arguments_fail_cleanly(gbf):
     d, c, T = H.frames(L, K, 1)[0]
     m.update(H.cuda(H.depth_m(d)), H.cuda(c), T)
     assert m.stats().allocated_blocks > 0
+
+
+def test_block_coordinates_out_of_range_are_flagged(gbf):
+    """Blocks beyond the 21-bit key range (|block coordinate| >= 2^20: 84 km at
+    1 cm voxels) are not allocated; the session raises COORD_RANGE and stays
+    usable."""
+    L = gbf
+    K = H.intrinsics(L)
+    m = L.DenseMapping(K, H.small_config(L, 0))
+    d, c, T = H.frames(L, K, 1)[0]
+    far = np.array(T, np.float64)
+    far[0, 3] += 9.0e4  # 90 km along x
+    m.update(H.cuda(H.depth_m(d)), H.cuda(c), far)
+    st = m.stats()
+    assert st.status & L.FLAG_COORD_RANGE
+    assert st.allocated_blocks == 0
+    m.update(H.cuda(H.depth_m(d)), H.cuda(c), T)  # back in range: fuses as usual
+    assert m.stats().allocated_blocks > 0

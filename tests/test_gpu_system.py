@@ -348,3 +348,44 @@ def test_ray_tile_same_raycast(gbf, tile_w):
     for x, y in zip(H.sort_blocks(*out[0][1]), H.sort_blocks(*out[1][1])):
         assert np.array_equal(x, y)
     assert np.array_equal(np.nan_to_num(out[0][2], nan=7.0), np.nan_to_num(out[1][2], nan=7.0))
+
+
+def test_inactive_slot_skips_its_ticks(gbf):
+    """A slot marked inactive for some ticks is left as it was: its session
+    ends equal to the same session fed only its active frames, and its
+    neighbour is undisturbed."""
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 1)
+    fa = H.frames(L, K, 5, seed=50)
+    fb = H.frames(L, K, 5, seed=51)
+    skip = {1, 2}  # ticks on which slot 1 is inactive
+
+    def alone(fr, ticks):
+        s = L.System(K, cfg)
+        s.set_pose(fr[0][2])
+        for k in ticks:
+            s.process_images(H.cuda(fr[k][0]), H.cuda(fr[k][1]))
+        torch.cuda.synchronize()
+        return s.get_camera_pose(), s.export()
+
+    a, b = L.System(K, cfg), L.System(K, cfg)
+    a.set_pose(fa[0][2])
+    b.set_pose(fb[0][2])
+    batch = L.FusionBatch(2)
+    batch.set(0, a)
+    batch.set(1, b)
+    for k in range(5):
+        a.stage(H.cuda(fa[k][0]), H.cuda(fa[k][1]))
+        if k not in skip:
+            b.stage(H.cuda(fb[k][0]), H.cuda(fb[k][1]))
+        batch.process([True, k not in skip])
+    batch.flush()
+    torch.cuda.synchronize()
+    for sess, (pose, m) in ((a, alone(fa, range(5))), (b, alone(fb, [k for k in range(5) if k not in skip]))):
+        assert np.array_equal(sess.get_camera_pose(), pose)
+        for x, y in zip(H.sort_blocks(*sess.export()), H.sort_blocks(*m)):
+            assert np.array_equal(x, y)
+    assert b.stats().frame_index == 3 and a.stats().frame_index == 5
+    batch.close()
