@@ -172,8 +172,9 @@ GBF_API gbf_status gbf_get_stats(gbf_session *s, gbf_frame_stats *out, void *str
 
 /* ---- mapping ------------------------------------------------------------------ */
 /* Allocate blocks along every valid pixel's truncation band, enumerate visible
- * blocks and integrate TSDF + colour.  depth: float metres.  rgb: 3 bytes/px.
- * nmap != NULL selects the normal-weighted update (update_map_weighted_kernel,
+ * blocks and integrate TSDF + colour.  depth: float metres (rows 4-byte aligned).
+ * rgb: 3 bytes/px.  nmap (float4, rows 16-byte aligned) != NULL selects the
+ * normal-weighted update (update_map_weighted_kernel,
  * depth_fusion.cu:356-428), NULL the 1/d^2 update (update_map_with_colour_kernel,
  * depth_fusion.cu:288-354). */
 GBF_API gbf_status gbf_fuse(gbf_session *s, const float *depth_dev, int64_t depth_pitch,
@@ -181,10 +182,24 @@ GBF_API gbf_status gbf_fuse(gbf_session *s, const float *depth_dev, int64_t dept
                             const float *nmap_dev, int64_t nmap_pitch,
                             const double T_wc[16], void *stream);
 /* z-range tiles from the last fuse's visible blocks, then a per-pixel raycast
- * into vmap (float4 per pixel, NaN = no hit).  As in the reference, vmap is left
- * untouched when the last fuse saw no visible / renderable block. */
+ * into vmap (float4 per pixel, NaN = no hit; rows 16-byte aligned).  As in the
+ * reference, vmap is left untouched when the last fuse saw no visible /
+ * renderable block. */
 GBF_API gbf_status gbf_raycast(gbf_session *s, const double T_wc[16],
                                float *vmap_dev, int64_t vmap_pitch, void *stream);
+/* gbf_raycast plus, when given, the model normals and colours:
+ *   nmap (float4 per pixel, rows 16-byte aligned): computeNMapK
+ *     (src/tracking/cuda_imgproc.cu:276-305) of the vertex map, the normals the
+ *     reference's next frame tracks against;
+ *   rgb (3 bytes per pixel): the colour raycast_with_colour
+ *     (src/voxel_hashing/ray_tracing.cu:478-564) means to write -- a hit's nearest
+ *     voxel colour (read_colour, :427-441), white where there is no hit or that
+ *     voxel is unobserved.  (The reference's host call runs the plain raycast
+ *     instead and writes no colour; the vertex map here keeps the plain raycast's
+ *     hits.) */
+GBF_API gbf_status gbf_raycast_maps(gbf_session *s, const double T_wc[16], float *vmap_dev, int64_t vmap_pitch,
+                                    float *nmap_dev, int64_t nmap_pitch, uint8_t *rgb_dev, int64_t rgb_pitch,
+                                    void *stream);
 /* DenseMapping::raycast_check_visibility (src/voxel_hashing/voxel_hashing.cpp:121-135):
  * the visible-block list recomputed for pose T by the frustum test alone
  * (count_visible_entry, src/voxel_hashing/ray_tracing.cu:778-807) over every
@@ -222,7 +237,11 @@ GBF_API gbf_status gbf_build_pyramid(gbf_session *s, int32_t which, const float 
 GBF_API gbf_status gbf_reduce(gbf_session *s, int32_t level, const double T[16], float stddev,
                               double out[58], void *stream);
 /* Level-0 images of a reference and a current frame, owned by the caller (dense
- * rows; vertex / normal maps float4 per pixel, intensities and gradients float). */
+ * rows; vertex / normal maps float4 per pixel, intensities and gradients float).
+ * The vertex and normal maps and the reference intensity start on 16-byte
+ * boundaries, the other images on 4-byte boundaries (GBF_ERR_INVALID_ARG
+ * otherwise); the reference intensity is read in 16-byte chunks, so up to 12
+ * bytes past its last pixel, which a cudaMalloc'd image always has. */
 typedef struct gbf_reduce_inputs {
     int32_t width, height;
     float fx, fy, cx, cy;

@@ -117,6 +117,15 @@ class DenseMapping : public Session {
     void raycast(DeviceImageView &vmap, const Pose &pose, void *stream = nullptr) {
         check(gbf_raycast(handle(), pose.data(), (float *)vmap.data, vmap.pitch, stream), "DenseMapping::raycast");
     }
+    // raycast(vmap, image, pose) (voxel_hashing.h:20): the vertex map plus the
+    // hits' voxel colours (RGB888) in image; nmap, when given, the model normals
+    void raycast(DeviceImageView &vmap, DeviceImageView &image, const Pose &pose, DeviceImageView *nmap = nullptr,
+                 void *stream = nullptr) {
+        check(gbf_raycast_maps(handle(), pose.data(), (float *)vmap.data, vmap.pitch,
+                               nmap ? (float *)nmap->data : nullptr, nmap ? nmap->pitch : 0,
+                               (uint8_t *)image.data, image.pitch, stream),
+              "DenseMapping::raycast");
+    }
     void reset_mapping(void *stream = nullptr) { check(gbf_session_reset(handle(), stream), "reset_mapping"); }
     // mesh buffers are caller-allocated device memory of max_tris triangles (system.h:36-41)
     size_t fetch_mesh_vertex_only(void *vertex, size_t max_tris) {

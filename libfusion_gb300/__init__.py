@@ -165,8 +165,15 @@ class DenseMapping(_Session):
         call("gbf_fuse", self._h, _ptr(depth), W * 4, _ptr(image), W * 3, _ptr(normal), W * 16, mat16(pose),
              _stream(stream))
 
-    def raycast(self, vmap, pose, stream=None) -> None:
-        call("gbf_raycast", self._h, mat16(pose), _ptr(vmap), self.K.width * 16, _stream(stream))
+    def raycast(self, vmap, pose, nmap=None, rgb=None, stream=None) -> None:
+        """Raycast at `pose` into `vmap` (H, W, 4); with `nmap` (H, W, 4) the model
+        normals, with `rgb` (H, W, 3) uint8 the hits' voxel colours (white elsewhere)."""
+        if nmap is None and rgb is None:
+            call("gbf_raycast", self._h, mat16(pose), _ptr(vmap), self.K.width * 16, _stream(stream))
+            return
+        call("gbf_raycast_maps", self._h, mat16(pose), _ptr(vmap), self.K.width * 16,
+             None if nmap is None else _ptr(nmap), self.K.width * 16,
+             None if rgb is None else _ptr(rgb), self.K.width * 3, _stream(stream))
 
     def raycast_check_visibility(self, vmap, pose, stream=None) -> None:
         """Visible blocks recomputed for `pose` (frustum test over every allocated

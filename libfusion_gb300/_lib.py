@@ -118,6 +118,7 @@ SIGNATURES = {
     "gbf_get_stats": (C.c_int, [_P, C.POINTER(FrameStats), _P]),
     "gbf_fuse": (C.c_int, [_P, _P, _I64, _P, _I64, _P, _I64, _D16, _P]),
     "gbf_raycast": (C.c_int, [_P, _D16, _P, _I64, _P]),
+    "gbf_raycast_maps": (C.c_int, [_P, _D16, _P, _I64, _P, _I64, _P, _I64, _P]),
     "gbf_extract_mesh": (C.c_int, [_P, _I32, _P, _P, _U64, C.POINTER(C.c_uint64), _P]),
     "gbf_build_pyramid": (C.c_int, [_P, _I32, _P, _I64, _P, _I64, _P]),
     "gbf_reduce": (C.c_int, [_P, _I32, _D16, C.c_float, _D16, _P]),

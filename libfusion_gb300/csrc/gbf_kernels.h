@@ -56,11 +56,16 @@ void launch_integrate(const SessionView *d_sv, int nslots, const Extent &ex, int
                       cudaStream_t st);
 
 // ---- raycast (raycast.cu) -------------------------------------------------------
+// rgb_ext (optional): the hits' nearest voxel colours, 3 bytes per pixel, white elsewhere
 void launch_raycast(const SessionView *d_sv, int nslots, const Extent &ex, float4 *vmap_ext, long long vmap_pitch,
-                    int post_pyramid, const int *layouts, cudaStream_t st);
+                    int post_pyramid, const int *layouts, cudaStream_t st, uint8_t *rgb_ext = nullptr,
+                    long long rgb_pitch = 0);
 void launch_zrange(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st);
 void launch_march(const SessionView *d_sv, int nslots, const Extent &ex, float4 *vmap_ext, long long vmap_pitch,
-                  const int *layouts, cudaStream_t st);
+                  const int *layouts, cudaStream_t st, uint8_t *rgb_ext = nullptr, long long rgb_pitch = 0);
+// computeNMapK (cuda_imgproc.cu:276-305) of a pitched vertex map into a pitched normal map
+void launch_nmap_of(const float4 *vmap, long long vmap_pitch, float4 *nmap, long long nmap_pitch, int w, int h,
+                    cudaStream_t st);
 void launch_post(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st);
 
 // ---- tracking (tracking.cu) -----------------------------------------------------

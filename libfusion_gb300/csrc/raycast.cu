@@ -224,7 +224,8 @@ constexpr int kMaxMarch = 1 << 16;  // safety bound; the march advances >= 1 vox
 
 template <int LAYOUT>
 __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionView *__restrict__ svs, float4 *vmap_ext,
-                                                                  long long vmap_pitch, int tw) {
+                                                                  long long vmap_pitch, int tw, uint8_t *rgb_ext,
+                                                                  long long rgb_pitch) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active || sv.layout != LAYOUT) return;
     // the reference skips the raycast when nothing was visible or renderable
@@ -246,6 +247,10 @@ __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionV
                            : sv.vmap[sv.ts->idx][0] + (size_t)y * K.w + x;
     const float qnan = __int_as_float(0x7fffffff);
     *out = make_float4(qnan, qnan, qnan, qnan);
+    // colour (raycast_with_colour, ray_tracing.cu:478-564): white unless a hit's
+    // nearest voxel has been observed
+    uint8_t *rgb_px = rgb_ext ? rgb_ext + y * rgb_pitch + (long long)x * 3 : nullptr;
+    if (rgb_px) rgb_px[0] = rgb_px[1] = rgb_px[2] = 255;
 
     const int cx = __float2int_rd((float)x / 8), cy = __float2int_rd((float)y / 8);
     if (cx >= sv.zr_w || cy >= sv.zr_h) return;
@@ -296,6 +301,21 @@ __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionV
     if (found) {
         const float3 c = Tcw.apply(r.x * sv.voxel, r.y * sv.voxel, r.z * sv.voxel);
         *out = make_float4(c.x, c.y, c.z, 1.0f);
+        if (rgb_px) {  // read_colour (ray_tracing.cu:427-441): the voxel ToVector3i(pt)
+            const int vx = floor_ref(r.x), vy = floor_ref(r.y), vz = floor_ref(r.z);
+            const int id = bc.get(mv, voxel_to_block(vx), voxel_to_block(vy), voxel_to_block(vz));
+            if (id >= 0) {
+                const int i = id * kBlockVoxels + (voxel_to_local(vz) * 64 + voxel_to_local(vy) * 8 + voxel_to_local(vx));
+                bool observed;
+                sdf_at<LAYOUT>(mv, i, observed);
+                if (observed) {
+                    const uchar4 col = sv.vox_rgb[i];
+                    rgb_px[0] = col.x;
+                    rgb_px[1] = col.y;
+                    rgb_px[2] = col.z;
+                }
+            }
+        }
     }
 }
 
@@ -316,6 +336,32 @@ __global__ void vmap_down_kernel(const SessionView *__restrict__ svs, int level)
 }
 
 // computeNMapK (cuda_imgproc.cu:276-294) over every level of the reference set
+// computeNMapK (cuda_imgproc.cu:276-305) at (x, y) of a vertex map whose rows are
+// `stride` float4 apart: normalised cross product of the horizontal and vertical
+// differences; NaN in the last row and column (written, where the reference
+// leaves them unwritten) and wherever a neighbour is NaN.
+__device__ __forceinline__ float4 normal_at(const float4 *V, long long stride, int x, int y, int w, int h) {
+    const float qnan = __int_as_float(0x7fffffff);
+    if (x >= w - 1 || y >= h - 1) return make_float4(qnan, qnan, qnan, qnan);
+    const int x10 = max(x - 1, 0), y10 = max(y - 1, 0);
+    const float4 v00 = V[y * stride + x10], v01 = V[y * stride + x + 1];
+    const float4 v10 = V[y10 * stride + x], v11 = V[(y + 1) * stride + x];
+    const float3 a = make_float3(v01.x - v00.x, v01.y - v00.y, v01.z - v00.z);
+    const float3 bb = make_float3(v11.x - v10.x, v11.y - v10.y, v11.z - v10.z);
+    const float3 n = cross3(a, bb);
+    const float l = norm3(n.x, n.y, n.z);
+    return make_float4(n.x / l, n.y / l, n.z / l, 1.f);
+}
+
+__global__ void nmap_of_kernel(const float4 *vmap, long long vmap_pitch, float4 *nmap, long long nmap_pitch, int w,
+                               int h) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= w || y >= h) return;
+    // the pitches are multiples of 16 bytes (checked by the caller)
+    reinterpret_cast<float4 *>(reinterpret_cast<char *>(nmap) + y * nmap_pitch)[x] =
+        normal_at(vmap, vmap_pitch / 16, x, y, w, h);
+}
+
 __global__ void nmap_all_kernel(const SessionView *__restrict__ svs) {
     const SessionView &sv = svs[blockIdx.y];
     if (!sv.active) return;
@@ -331,20 +377,7 @@ __global__ void nmap_all_kernel(const SessionView *__restrict__ svs) {
     if (i >= w * h) return;
     const int x = i % w, y = i / w;
     const int set = sv.ts->idx;
-    const float4 *V = sv.vmap[set][level];
-    const float qnan = __int_as_float(0x7fffffff);
-    if (x < w - 1 && y < h - 1) {
-        const int x10 = max(x - 1, 0), y10 = max(y - 1, 0);
-        const float4 v00 = V[(size_t)y * w + x10], v01 = V[(size_t)y * w + x + 1];
-        const float4 v10 = V[(size_t)y10 * w + x], v11 = V[(size_t)(y + 1) * w + x];
-        const float3 a = make_float3(v01.x - v00.x, v01.y - v00.y, v01.z - v00.z);
-        const float3 bb = make_float3(v11.x - v10.x, v11.y - v10.y, v11.z - v10.z);
-        const float3 n = cross3(a, bb);
-        const float l = norm3(n.x, n.y, n.z);
-        sv.nmap[set][level][i] = make_float4(n.x / l, n.y / l, n.z / l, 1.f);
-    } else {
-        sv.nmap[set][level][i] = make_float4(qnan, qnan, qnan, qnan);
-    }
+    sv.nmap[set][level][i] = normal_at(sv.vmap[set][level], w, x, y, w, h);
 }
 
 }  // namespace
@@ -357,16 +390,21 @@ void launch_zrange(const SessionView *d_sv, int nslots, const Extent &ex, cudaSt
 }
 
 void launch_march(const SessionView *d_sv, int nslots, const Extent &ex, float4 *vmap_ext, long long vmap_pitch,
-                  const int *layouts, cudaStream_t st) {
+                  const int *layouts, cudaStream_t st, uint8_t *rgb_ext, long long rgb_pitch) {
     const int tw = ray_tile_width(ex), th = kRayThreads / tw;
     // every slot's tiles fit: a smaller frame has fewer tiles per row and per column
     const dim3 g(((ex.w + tw - 1) / tw) * ((ex.h + th - 1) / th), nslots);
     if (layouts[GBF_VOXEL_REF])
-        raycast_kernel<GBF_VOXEL_REF><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw);
+        raycast_kernel<GBF_VOXEL_REF><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, rgb_ext, rgb_pitch);
     if (layouts[GBF_VOXEL_HALF])
-        raycast_kernel<GBF_VOXEL_HALF><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw);
+        raycast_kernel<GBF_VOXEL_HALF><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, rgb_ext, rgb_pitch);
     if (layouts[GBF_VOXEL_SNORM])
-        raycast_kernel<GBF_VOXEL_SNORM><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw);
+        raycast_kernel<GBF_VOXEL_SNORM><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, rgb_ext, rgb_pitch);
+}
+
+void launch_nmap_of(const float4 *vmap, long long vmap_pitch, float4 *nmap, long long nmap_pitch, int w, int h,
+                    cudaStream_t st) {
+    nmap_of_kernel<<<dim3((w + 127) / 128, h), 128, 0, st>>>(vmap, vmap_pitch, nmap, nmap_pitch, w, h);
 }
 
 void launch_post(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {
@@ -380,9 +418,9 @@ void launch_post(const SessionView *d_sv, int nslots, const Extent &ex, cudaStre
 }
 
 void launch_raycast(const SessionView *d_sv, int nslots, const Extent &ex, float4 *vmap_ext, long long vmap_pitch,
-                    int post_pyramid, const int *layouts, cudaStream_t st) {
+                    int post_pyramid, const int *layouts, cudaStream_t st, uint8_t *rgb_ext, long long rgb_pitch) {
     launch_zrange(d_sv, nslots, ex, st);
-    launch_march(d_sv, nslots, ex, vmap_ext, vmap_pitch, layouts, st);
+    launch_march(d_sv, nslots, ex, vmap_ext, vmap_pitch, layouts, st, rgb_ext, rgb_pitch);
     if (post_pyramid) launch_post(d_sv, nslots, ex, st);
 }
 

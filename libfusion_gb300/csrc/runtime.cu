@@ -573,12 +573,20 @@ GBF_API gbf_status gbf_get_stats(gbf_session *s, gbf_frame_stats *out, void *str
     return GBF_OK;
 }
 
+// A kernel reads or writes a caller's image as rows of `elem`-byte elements:
+// its base address and its pitch must both be multiples of elem.
+static bool rows_aligned(const void *p, int64_t pitch, int elem) {
+    return reinterpret_cast<uintptr_t>(p) % elem == 0 && pitch % elem == 0;
+}
+
 GBF_API gbf_status gbf_fuse(gbf_session *s, const float *depth, int64_t depth_pitch, const uint8_t *rgb,
                             int64_t rgb_pitch, const float *nmap, int64_t nmap_pitch, const double T[16],
                             void *stream) {
     if (!s || !depth || !rgb || !T) return set_error(GBF_ERR_INVALID_ARG, "gbf_fuse: null");
     if (depth_pitch < s->K.width * 4 || rgb_pitch < s->K.width * 3 || (nmap && nmap_pitch < s->K.width * 16))
         return set_error(GBF_ERR_INVALID_ARG, "gbf_fuse: pitch smaller than a row");
+    if (!rows_aligned(depth, depth_pitch, 4) || (nmap && !rows_aligned(nmap, nmap_pitch, 16)))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_fuse: depth rows must be 4-byte and normal rows 16-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
     gbf_status r = set_map_pose(s, T, st);
     if (r != GBF_OK) return r;
@@ -591,6 +599,8 @@ GBF_API gbf_status gbf_fuse(gbf_session *s, const float *depth, int64_t depth_pi
 GBF_API gbf_status gbf_raycast(gbf_session *s, const double T[16], float *vmap, int64_t vmap_pitch, void *stream) {
     if (!s || !T || !vmap) return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast: null");
     if (vmap_pitch < s->K.width * 16) return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast: pitch smaller than a row");
+    if (!rows_aligned(vmap, vmap_pitch, 16))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast: vertex-map rows must be 16-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
     gbf_status r = set_map_pose(s, T, st);
     if (r != GBF_OK) return r;
@@ -598,11 +608,32 @@ GBF_API gbf_status gbf_raycast(gbf_session *s, const double T[16], float *vmap, 
     return check_cuda("gbf_raycast");
 }
 
+GBF_API gbf_status gbf_raycast_maps(gbf_session *s, const double T[16], float *vmap, int64_t vmap_pitch,
+                                    float *nmap, int64_t nmap_pitch, uint8_t *rgb, int64_t rgb_pitch, void *stream) {
+    if (!s || !T || !vmap) return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast_maps: null");
+    const int W = s->K.width, H = s->K.height;
+    if (vmap_pitch < W * 16LL || (nmap && nmap_pitch < W * 16LL) || (rgb && rgb_pitch < W * 3LL))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast_maps: pitch smaller than a row");
+    if (!rows_aligned(vmap, vmap_pitch, 16) || (nmap && !rows_aligned(nmap, nmap_pitch, 16)))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast_maps: vertex and normal rows must be 16-byte aligned");
+    cudaStream_t st = (cudaStream_t)stream;
+    gbf_status r = set_map_pose(s, T, st);
+    if (r != GBF_OK) return r;
+    launch_raycast(s->d_view, 1, s->ex, reinterpret_cast<float4 *>(vmap), vmap_pitch, 0, s->layouts, st, rgb,
+                   rgb_pitch);
+    if (nmap)
+        launch_nmap_of(reinterpret_cast<const float4 *>(vmap), vmap_pitch, reinterpret_cast<float4 *>(nmap),
+                       nmap_pitch, W, H, st);
+    return check_cuda("gbf_raycast_maps");
+}
+
 GBF_API gbf_status gbf_raycast_check_visibility(gbf_session *s, const double T[16], float *vmap, int64_t vmap_pitch,
                                                 void *stream) {
     if (!s || !T || !vmap) return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast_check_visibility: null");
     if (vmap_pitch < s->K.width * 16)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast_check_visibility: pitch smaller than a row");
+    if (!rows_aligned(vmap, vmap_pitch, 16))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_raycast_check_visibility: vertex-map rows must be 16-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
     gbf_status r = set_map_pose(s, T, st);
     if (r != GBF_OK) return r;
@@ -619,6 +650,8 @@ GBF_API gbf_status gbf_render_scene(const float *vmap, int64_t vmap_pitch, const
     if (vmap_pitch < width * 16LL || nmap_pitch < width * 16LL || out_pitch < width * 4LL ||
         (rgb && rgb_pitch < width * 3LL))
         return set_error(GBF_ERR_INVALID_ARG, "gbf_render_scene: pitch smaller than a row");
+    if (!rows_aligned(vmap, vmap_pitch, 16) || !rows_aligned(nmap, nmap_pitch, 16) || !rows_aligned(out, out_pitch, 4))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_render_scene: map rows must be 16-byte and output rows 4-byte aligned");
     launch_render(reinterpret_cast<const float4 *>(vmap), vmap_pitch, reinterpret_cast<const float4 *>(nmap),
                   nmap_pitch, rgb, rgb_pitch, 3, width, height, reinterpret_cast<uchar4 *>(out), out_pitch,
                   (cudaStream_t)stream);
@@ -630,6 +663,8 @@ GBF_API gbf_status gbf_session_render(gbf_session *s, int32_t textured, uint8_t 
     if (!s || !out) return set_error(GBF_ERR_INVALID_ARG, "gbf_session_render: null");
     const int W = s->K.width, H = s->K.height;
     if (out_pitch < W * 4LL) return set_error(GBF_ERR_INVALID_ARG, "gbf_session_render: pitch smaller than a row");
+    if (!rows_aligned(out, out_pitch, 4))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_session_render: output rows must be 4-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
     // the reference frame's maps: the model prediction of the last raycast
     int idx = 0;
@@ -666,6 +701,8 @@ GBF_API gbf_status gbf_build_pyramid(gbf_session *s, int32_t which, const float 
     if (which != 0 && which != 1) return set_error(GBF_ERR_INVALID_ARG, "gbf_build_pyramid: which must be 0 or 1");
     if (depth_pitch < s->K.width * 4 || rgb_pitch < s->K.width * 3)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_build_pyramid: pitch smaller than a row");
+    if (!rows_aligned(depth, depth_pitch, 4))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_build_pyramid: depth rows must be 4-byte aligned");
     IngestArgs a{which, 2, depth, depth_pitch, rgb, rgb_pitch};
     launch_ingest(s->d_view, 1, s->ex, a, (cudaStream_t)stream);
     return check_cuda("gbf_build_pyramid");
@@ -739,6 +776,8 @@ GBF_API gbf_status gbf_process_frame(gbf_session *s, const uint16_t *depth, int6
     if (!s || !depth || !rgb) return set_error(GBF_ERR_INVALID_ARG, "gbf_process_frame: null");
     if (depth_pitch < s->K.width * 2 || rgb_pitch < s->K.width * 3)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_process_frame: pitch smaller than a row");
+    if (!rows_aligned(depth, depth_pitch, 2))
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_process_frame: depth rows must be 2-byte aligned");
     IngestArgs a{0, 1, depth, depth_pitch, rgb, rgb_pitch};
     enqueue_frame(s->d_view, 1, s->ex, s->layouts, a, (cudaStream_t)stream);
     return check_cuda("gbf_process_frame");

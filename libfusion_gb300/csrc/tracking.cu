@@ -860,6 +860,14 @@ extern "C" GBF_API gbf_status gbf_reduce_noalloc(const gbf_reduce_inputs *in, co
         return set_error(GBF_ERR_INVALID_ARG, "gbf_reduce_noalloc: null pointer");
     if (in->width < 8 || in->height < 8 || !(in->fx > 0) || !(in->fy > 0))
         return set_error(GBF_ERR_INVALID_ARG, "gbf_reduce_noalloc: bad image size or focal length");
+    // the reference images are staged in 16-byte copies, the vertex and normal
+    // maps read as float4, the other images as float
+    auto aligned = [](const void *p, uintptr_t n) { return reinterpret_cast<uintptr_t>(p) % n == 0; };
+    if (!aligned(in->ref_vmap, 16) || !aligned(in->ref_nmap, 16) || !aligned(in->ref_intensity, 16) ||
+        !aligned(in->cur_vmap, 16) || !aligned(in->cur_nmap, 16) || !aligned(in->cur_intensity, 4) ||
+        !aligned(in->cur_didx, 4) || !aligned(in->cur_didy, 4))
+        return set_error(GBF_ERR_INVALID_ARG,
+                         "gbf_reduce_noalloc: vertex, normal and reference intensity images must be 16-byte aligned");
     const long long pixels = (long long)in->width * in->height;
     if (pixels > (long long)kStaticReduceCtas * kReduceThreads * kReducePixelsPerThread)
         return set_error(GBF_ERR_CAPACITY, "gbf_reduce_noalloc: at most 2,097,152 pixels per image");

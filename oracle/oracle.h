@@ -70,6 +70,8 @@ typedef struct or_system_f64 or_system_f64;
     int or_fuse_##S(or_map_##S *m, const float *depth, const uint8_t *rgb, const float *nmap, const double T[16]); \
     /* DenseMapping::raycast: z-range tiles of the last fuse's visible blocks + march; vmap float4 */              \
     int or_raycast_##S(or_map_##S *m, const double T[16], float *vmap);                                            \
+    /* the same, plus the hit's nearest voxel colour (3 bytes per pixel, white elsewhere) */                     \
+    int or_raycast_maps_##S(or_map_##S *m, const double T[16], float *vmap, uint8_t *rgb);                        \
     /* DenseMapping::raycast_check_visibility: visible list recomputed for T, then raycast */                      \
     int or_raycast_check_visibility_##S(or_map_##S *m, const double T[16], float *vmap);                           \
     int64_t or_map_blocks_##S(const or_map_##S *m);                                                                \

@@ -78,6 +78,7 @@ def lib() -> C.CDLL:
                 f"or_frame_set_vmap_{s}": (None, [P, P]),
                 f"or_reduce_{s}": (None, [P, P, C.c_int, C.POINTER(C.c_float), C.c_float, D]),
                 f"or_reduce_terms_{s}": (None, [P, P, C.c_int, C.POINTER(C.c_float), C.c_float, P]),
+                f"or_raycast_maps_{s}": (C.c_int, [P, D, P, P]),
                 f"or_track_{s}": (None, [P, P, D, C.POINTER(OrTrackResult)]),
                 f"or_system_create_{s}": (P, [C.POINTER(OrConfig), C.POINTER(OrIntrinsics)]),
                 f"or_system_destroy_{s}": (None, [P]),
@@ -164,6 +165,13 @@ class OracleMap:
             vmap = np.full((self.K.height, self.K.width, 4), np.nan, np.float32)
         self.fn("or_raycast")(self.h, _d16(pose), _p(vmap))
         return vmap
+
+    def raycast_maps(self, pose):
+        """Vertex map and the hits' nearest voxel colours (white elsewhere)."""
+        vmap = np.full((self.K.height, self.K.width, 4), np.nan, np.float32)
+        rgb = np.full((self.K.height, self.K.width, 3), 255, np.uint8)
+        self.fn("or_raycast_maps")(self.h, _d16(pose), _p(vmap), _p(rgb))
+        return vmap, rgb
 
     def raycast_check_visibility(self, pose, vmap: np.ndarray | None = None) -> np.ndarray:
         """DenseMapping::raycast_check_visibility: visible list for `pose`, then raycast."""

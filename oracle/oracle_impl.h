@@ -532,9 +532,25 @@ static R read_interp(const MAP *m, R px, R py, R pz, int *valid) {
 }
 
 /* MapRenderingDelegate::operator() (ray_tracing.cu:346-425) */
-static void ray_pixel(const MAP *m, const M34 *Twc, const M34 *Tcw, int x, int y, float *out) {
+/* read_colour (ray_tracing.cu:427-441): the colour of the voxel ToVector3i(pt),
+ * valid when its weight is not 0 */
+static int read_colour(const MAP *m, R px, R py, R pz, uint8_t *rgb) {
+    const int vx = floor_r(px), vy = floor_r(py), vz = floor_r(pz);
+    const int id = map_find(m, vtob(vx), vtob(vy), vtob(vz));
+    if (id < 0) return 0;
+    const size_t i = (size_t)id * 512 + vtol(vz) * 64 + vtol(vy) * 8 + vtol(vx);
+    if (vox_w(m, i) == 0) return 0;
+    rgb[0] = m->rgb[i * 4]; rgb[1] = m->rgb[i * 4 + 1]; rgb[2] = m->rgb[i * 4 + 2];
+    return 1;
+}
+
+/* rgb (optional, 3 bytes): the colour raycast_with_colour (ray_tracing.cu:478-564)
+ * means to write -- the hit's nearest voxel colour, white (255) elsewhere; the
+ * vertex keeps the march's own validity, as the executed raycast does */
+static void ray_pixel(const MAP *m, const M34 *Twc, const M34 *Tcw, int x, int y, float *out, uint8_t *rgb) {
     const or_intrinsics *K = &m->K;
     out[0] = out[1] = out[2] = out[3] = NAN;
+    if (rgb) rgb[0] = rgb[1] = rgb[2] = 255;
     const int cx = floor_rd((R)x / (R)8), cy = floor_rd((R)y / (R)8);
     if (cx >= m->zr_w || cy >= m->zr_h) return;
     const R zr0 = m->zr_min[cy * m->zr_w + cx], zr1 = m->zr_max[cy * m->zr_w + cx];
@@ -582,10 +598,12 @@ static void ray_pixel(const MAP *m, const M34 *Twc, const M34 *Tcw, int x, int y
         if (g_rs) g_rs->hits++;
         const V3 c = m_apply(Tcw, r.x * m->voxel, r.y * m->voxel, r.z * m->voxel);
         out[0] = (float)c.x; out[1] = (float)c.y; out[2] = (float)c.z; out[3] = 1.0f;
+        uint8_t col[3];
+        if (rgb && read_colour(m, r.x, r.y, r.z, col)) { rgb[0] = col[0]; rgb[1] = col[1]; rgb[2] = col[2]; }
     }
 }
 
-int SFX(or_raycast)(MAP *m, const double T[16], float *vmap) {
+int SFX(or_raycast_maps)(MAP *m, const double T[16], float *vmap, uint8_t *rgb) {
     set_threads(m->cfg.threads);
     double inv[12];
     pose_inv(T, inv);
@@ -597,9 +615,12 @@ int SFX(or_raycast)(MAP *m, const double T[16], float *vmap) {
     const int W = m->K.width, H = m->K.height;
 #pragma omp parallel for schedule(dynamic, 2)
     for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x) ray_pixel(m, &Twc, &Tcw, x, y, vmap + ((size_t)y * W + x) * 4);
+        for (int x = 0; x < W; ++x)
+            ray_pixel(m, &Twc, &Tcw, x, y, vmap + ((size_t)y * W + x) * 4, rgb ? rgb + ((size_t)y * W + x) * 3 : NULL);
     return 1;
 }
+
+int SFX(or_raycast)(MAP *m, const double T[16], float *vmap) { return SFX(or_raycast_maps)(m, T, vmap, NULL); }
 
 /* DenseMapping::raycast_check_visibility (voxel_hashing.cpp:121-135): the visible
  * list recomputed for pose T by count_visible_entry (ray_tracing.cu:778-807) --
@@ -637,7 +658,7 @@ void SFX(or_ray_stats)(MAP *m, const double T[16], long long out[7], int32_t *st
         for (int y = 0; y < m->K.height; ++y)
             for (int x = 0; x < m->K.width; ++x) {
                 const long long s0 = rs.steps + rs.interps * 8;
-                ray_pixel(m, &Twc, &Tcw, x, y, px);
+                ray_pixel(m, &Twc, &Tcw, x, y, px, NULL);
                 if (steps_per_pixel) steps_per_pixel[y * m->K.width + x] = (int32_t)(rs.steps + rs.interps * 8 - s0);
             }
     g_rs = NULL;

@@ -118,3 +118,27 @@ def test_block_coordinates_out_of_range_are_flagged(gbf):
     assert st.allocated_blocks == 0
     m.update(H.cuda(H.depth_m(d)), H.cuda(c), T)  # back in range: fuses as usual
     assert m.stats().allocated_blocks > 0
+
+
+def test_misaligned_images_are_rejected(gbf):
+    """Images a kernel reads as float4 / float / u16 rows must start and step on
+    their element size: a misaligned pitch or pointer is an argument error,
+    not a device fault."""
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    m = L.DenseMapping(K, H.small_config(L, 0))
+    buf = torch.zeros(K.height * K.width * 4 + 64, device="cuda")
+    T = L._lib.mat16(np.eye(4))
+    with pytest.raises(L.GbfError, match="aligned"):  # vertex-map pitch not a multiple of 16
+        L._lib.call("gbf_raycast", m.handle, T, buf.data_ptr(), K.width * 16 + 4, None)
+    with pytest.raises(L.GbfError, match="aligned"):  # vertex map starting 4 bytes off
+        L._lib.call("gbf_raycast", m.handle, T, buf.data_ptr() + 4, K.width * 16, None)
+    rgb = torch.zeros(K.height * K.width * 3, dtype=torch.uint8, device="cuda")
+    with pytest.raises(L.GbfError, match="aligned"):  # depth pitch not a multiple of 4
+        L._lib.call("gbf_fuse", m.handle, buf.data_ptr(), K.width * 4 + 2, rgb.data_ptr(), K.width * 3, None, 0,
+                    T, None)
+    # the session is still usable
+    d, c, T2 = H.frames(L, K, 1)[0]
+    m.update(H.cuda(H.depth_m(d)), H.cuda(c), T2)
+    assert m.stats().allocated_blocks > 0

@@ -355,3 +355,45 @@ def test_large_room_figure_eight_bit_exact(gbf):
         osys.process(d, c)
         assert np.abs(s.get_camera_pose()[:3, 3] - osys.pose()[:3, 3]).max() < 1e-3
         assert s.stats().track.success == osys.last_result().success
+
+
+@pytest.mark.parametrize("layout", [0, 1, 2])
+def test_raycast_maps_bit_exact(gbf, layout):
+    """gbf_raycast_maps: the vertex map of gbf_raycast, the hits' nearest voxel
+    colours (raycast_with_colour's intent, white elsewhere) and the model
+    normals (computeNMapK of the vertex map), each bit-exact against the oracle."""
+    import oracle as O
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, layout)
+    m = L.DenseMapping(K, cfg)
+    om = _oracle_map(L, cfg, K)
+    fr = H.frames(L, K, 3, step=4)
+    for d, c, T in fr:
+        dm = H.depth_m(d)
+        m.update(H.cuda(dm), H.cuda(c), T)
+        om.fuse(dm, c, T)
+    T = fr[-1][2]
+    vm = torch.full((K.height, K.width, 4), float("nan"), device="cuda")
+    nm = torch.zeros((K.height, K.width, 4), device="cuda")
+    rgb = torch.zeros((K.height, K.width, 3), dtype=torch.uint8, device="cuda")
+    m.raycast(vm, T, nmap=nm, rgb=rgb)
+    g, gn, gc = vm.cpu().numpy(), nm.cpu().numpy(), rgb.cpu().numpy()
+    o, oc = om.raycast_maps(T)
+    gh, oh = ~np.isnan(g[..., 2]), ~np.isnan(o[..., 2])
+    assert np.array_equal(gh, oh) and gh.mean() > 0.8
+    assert np.array_equal(g[gh], o[oh])
+    assert np.array_equal(gc, oc)
+    coloured = np.any(gc != 255, axis=2)
+    assert coloured.sum() > 0.5 * gh.sum()  # most hits land on an observed voxel
+    assert np.all(gc[~gh] == 255)
+    fo = O.OracleFrame(O.config_from(cfg), O.intrinsics_from(K))
+    fo.set_vmap(g)
+    on = fo.get(1, 0)
+    assert np.array_equal(np.isnan(gn), np.isnan(on))
+    assert np.array_equal(gn[~np.isnan(gn)], on[~np.isnan(on)])
+    # the plain raycast's vertex map is the same
+    vm2 = torch.full((K.height, K.width, 4), float("nan"), device="cuda")
+    m.raycast(vm2, T)
+    assert np.array_equal(np.nan_to_num(vm2.cpu().numpy(), nan=7.0), np.nan_to_num(g, nan=7.0))
