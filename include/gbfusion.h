@@ -13,12 +13,15 @@
  * reference's Sophus::SE3d frame poses.  `stream` is a cudaStream_t passed as
  * void* (NULL = legacy default stream).
  *
- * Threading: a session, and a batch with the sessions in its slots, are driven
- * from one host thread at a time (calls on the same handle are not
- * synchronised).  Different sessions and batches may be used from different
- * threads concurrently.  A session in a batch is driven through the batch while
- * it sits there; it must outlive its slot (gbf_batch_set(b, slot, NULL) or
- * gbf_batch_destroy before gbf_session_destroy).
+ * Threading: a session is driven from one host thread at a time (calls on the
+ * same session are not synchronised); different sessions may be used from
+ * different threads concurrently.  A batch is internally synchronised: its
+ * calls may come from several threads -- camera threads staging frames while
+ * one thread runs the ticks and reads the results -- and each holds the batch's
+ * lock for its duration (gbf_batch_process and gbf_batch_results may wait
+ * there for an earlier tick).  A session in a batch is driven through the batch
+ * while it sits there; it must outlive its slot (gbf_batch_set(b, slot, NULL)
+ * or gbf_batch_destroy before gbf_session_destroy).
  *
  * Mapping of reference interfaces (paths relative to the reference project):
  *   DenseMapping::DenseMapping(K)          include/voxel_hashing/voxel_hashing.h:15   -> gbf_session_create

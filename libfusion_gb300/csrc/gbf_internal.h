@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <vector>
 
 #include "../../include/gbfusion.h"
@@ -52,6 +53,7 @@ struct gbf_session {
 };
 
 struct gbf_batch {
+    std::mutex mu;  // held by every gbf_batch_* call: a batch may be driven from several threads
     int max_slots = 0;
     std::vector<gbf_session *> sessions;
     std::vector<uint16_t *> in_depth;  // per-slot input override (device, dense)

@@ -970,6 +970,7 @@ static void batch_invalidate(gbf_batch *b) {
 
 GBF_API gbf_status gbf_batch_destroy(gbf_batch *b) {
     if (!b) return GBF_OK;
+    std::unique_lock<std::mutex> lock(b->mu);  // a call in flight on another thread ends first
     if (b->d_views_b) batch_flush(b, nullptr);  // the sessions outlive the batch: fuse what is owed
     cudaDeviceSynchronize();
     batch_invalidate(b);
@@ -1001,12 +1002,14 @@ GBF_API gbf_status gbf_batch_destroy(gbf_batch *b) {
     for (int k = 0; k < 2; ++k)
         for (int i = 0; i < 2; ++i)
             if (b->tev[k][i]) cudaEventDestroy(b->tev[k][i]);
+    lock.unlock();
     delete b;
     return check_cuda("gbf_batch_destroy");
 }
 
 GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
     if (!b || slot < 0 || slot >= b->max_slots) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set: bad slot");
+    std::lock_guard<std::mutex> lock(b->mu);
     gbf_status fs = batch_flush(b, nullptr);
     if (fs != GBF_OK) return fs;
     // a previous tick may still read the mirrors
@@ -1137,6 +1140,7 @@ static gbf_status batch_flush(gbf_batch *b, cudaStream_t st) {
 
 GBF_API gbf_status gbf_batch_flush(gbf_batch *b, void *stream) {
     if (!b) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_flush: null");
+    std::lock_guard<std::mutex> lock(b->mu);
     return batch_flush(b, (cudaStream_t)stream);
 }
 
@@ -1294,6 +1298,7 @@ gbf_status tune_step(gbf_batch *b, cudaStream_t st) {
 
 GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_t use_graph, void *stream) {
     if (!b || !active) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_process: null");
+    std::lock_guard<std::mutex> lock(b->mu);
     if (b->nslots == 0) return GBF_OK;
     {
         gbf_status ts = tune_step(b, (cudaStream_t)stream);
@@ -1397,6 +1402,7 @@ GBF_API gbf_status gbf_batch_stage(gbf_batch *b, int32_t slot, const uint16_t *d
                                    const uint8_t *rgb, int64_t rgb_pitch, void *stream) {
     if (!b || slot < 0 || slot >= b->max_slots || !depth || !rgb)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_stage: bad slot or pointers");
+    std::lock_guard<std::mutex> lock(b->mu);
     gbf_session *s = b->sessions[slot];
     if (!s) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_stage: empty slot");
     const int W = s->K.width, H = s->K.height;
@@ -1437,6 +1443,7 @@ GBF_API gbf_status gbf_batch_stage(gbf_batch *b, int32_t slot, const uint16_t *d
 GBF_API gbf_status gbf_batch_results(gbf_batch *b, int32_t back, gbf_slot_result *out, int32_t n) {
     if (!b || !out || n < 0 || back < 0 || back > 1)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_results: bad arguments");
+    std::lock_guard<std::mutex> lock(b->mu);
     if (b->submitted <= back) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_results: no such tick");
     const int k = back == 0 ? b->last : (b->last ^ 1);
     cudaError_t e = cudaEventSynchronize(b->ev[k]);
@@ -1448,6 +1455,7 @@ GBF_API gbf_status gbf_batch_results(gbf_batch *b, int32_t back, gbf_slot_result
 GBF_API gbf_status gbf_batch_set_inputs(gbf_batch *b, int32_t slot, const uint16_t *depth_dev, const uint8_t *rgb_dev) {
     if (!b || slot < 0 || slot >= b->max_slots || (!depth_dev) != (!rgb_dev))
         return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_inputs: bad slot or pointers");
+    std::lock_guard<std::mutex> lock(b->mu);
     b->in_depth[slot] = const_cast<uint16_t *>(depth_dev);
     b->in_rgb[slot] = const_cast<uint8_t *>(rgb_dev);
     return GBF_OK;
@@ -1463,6 +1471,7 @@ static void tune_off(gbf_batch *b) {
 GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups) {
     if (!b || groups < 1 || groups > gbf_batch::kMaxGroups)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_groups: 1..4 groups");
+    std::lock_guard<std::mutex> lock(b->mu);
     gbf_status fs = batch_flush(b, nullptr);
     if (fs != GBF_OK) return fs;
     for (int k = 0; k < 2; ++k)
@@ -1475,6 +1484,7 @@ GBF_API gbf_status gbf_batch_set_groups(gbf_batch *b, int32_t groups) {
 
 GBF_API gbf_status gbf_batch_set_stagger(gbf_batch *b, int32_t enable) {
     if (!b) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_stagger: null");
+    std::lock_guard<std::mutex> lock(b->mu);
     gbf_status fs = batch_flush(b, nullptr);
     if (fs != GBF_OK) return fs;
     for (int k = 0; k < 2; ++k)
@@ -1488,6 +1498,7 @@ GBF_API gbf_status gbf_batch_set_stagger(gbf_batch *b, int32_t enable) {
 GBF_API gbf_status gbf_batch_set_ray_tile(gbf_batch *b, int32_t tile_w) {
     if (!b || (tile_w != 4 && tile_w != 8 && tile_w != 16 && tile_w != 32))
         return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_ray_tile: tile width 4, 8, 16 or 32");
+    std::lock_guard<std::mutex> lock(b->mu);
     gbf_status fs = batch_flush(b, nullptr);
     if (fs != GBF_OK) return fs;
     for (int k = 0; k < 2; ++k)
@@ -1501,6 +1512,7 @@ GBF_API gbf_status gbf_batch_set_ray_tile(gbf_batch *b, int32_t tile_w) {
 
 GBF_API gbf_status gbf_batch_set_autotune(gbf_batch *b, int32_t enable, int32_t ticks_per_candidate) {
     if (!b) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_autotune: null");
+    std::lock_guard<std::mutex> lock(b->mu);
     if (enable && (ticks_per_candidate < 2 || ticks_per_candidate > 64))
         return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_autotune: 2..64 ticks per candidate");
     if (!enable) {
@@ -1522,6 +1534,7 @@ GBF_API gbf_status gbf_batch_set_autotune(gbf_batch *b, int32_t enable, int32_t 
 
 GBF_API gbf_status gbf_batch_tuning(gbf_batch *b, gbf_tuning *out) {
     if (!b || !out) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_tuning: null");
+    std::lock_guard<std::mutex> lock(b->mu);
     memset(out, 0, sizeof(*out));
     out->state = b->tune_on ? b->tune_state : 0;
     out->from_table = b->tune_on && b->tune_state == 2 ? b->tune_cached : 0;
@@ -1555,6 +1568,7 @@ GBF_API gbf_status gbf_autotune_forget(void) {
 
 GBF_API gbf_status gbf_batch_set_timing(gbf_batch *b, int32_t enable) {
     if (!b) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set_timing: null");
+    std::lock_guard<std::mutex> lock(b->mu);
     gbf_status fs = batch_flush(b, nullptr);
     if (fs != GBF_OK) return fs;
     for (int k = 0; k < 2; ++k)
@@ -1576,6 +1590,7 @@ GBF_API gbf_status gbf_batch_set_timing(gbf_batch *b, int32_t enable) {
 
 GBF_API gbf_status gbf_batch_phase_ms(gbf_batch *b, float *ms, int32_t n) {
     if (!b || !ms || n < kPhases) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_phase_ms: need 7 floats");
+    std::lock_guard<std::mutex> lock(b->mu);
     if (!b->timing) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_phase_ms: timing not enabled");
     for (int k = 0; k < 2; ++k)
         if (b->pending[k]) {
@@ -1590,6 +1605,7 @@ GBF_API gbf_status gbf_batch_phase_ms(gbf_batch *b, float *ms, int32_t n) {
 
 GBF_API gbf_status gbf_batch_kernels(gbf_batch *b, int32_t *n) {
     if (!b || !n) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_kernels: null");
+    std::lock_guard<std::mutex> lock(b->mu);
     int total = 0;
     const int groups = std::max(1, std::min(b->groups, b->nslots));
     for (int g = 0; g < groups; ++g)

@@ -389,3 +389,63 @@ def test_inactive_slot_skips_its_ticks(gbf):
             assert np.array_equal(x, y)
     assert b.stats().frame_index == 3 and a.stats().frame_index == 5
     batch.close()
+
+
+def test_batch_calls_from_several_threads(gbf):
+    """The batch is internally synchronised: camera threads stage their own
+    session's frames from pinned host memory, a monitor thread reads the tuner
+    and launch counts, and the main thread runs the ticks and reads results;
+    every session ends bit-identical to the same frames processed alone."""
+    import threading
+
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 1)
+    n, ticks = 4, 6
+    fr = [H.frames(L, K, ticks, seed=80 + i) for i in range(n)]
+    host = [[(torch.from_numpy(d).pin_memory(), torch.from_numpy(c).pin_memory()) for d, c, _ in f] for f in fr]
+    ss = [L.System(K, cfg) for _ in range(n)]
+    for s, f in zip(ss, fr):
+        s.set_pose(f[0][2])
+    batch = L.FusionBatch(n)
+    for i, s in enumerate(ss):
+        batch.set(i, s)
+    batch.autotune(True, 2)
+    stop = threading.Event()
+    seen = []
+
+    def monitor():
+        while not stop.is_set():
+            seen.append((batch.tuning()["state"], batch.kernels_per_tick()))
+
+    mon = threading.Thread(target=monitor)
+    mon.start()
+    streams = [torch.cuda.Stream() for _ in range(n)]
+    try:
+        for k in range(ticks):
+            def stage(i):
+                batch.stage(i, host[i][k][0], host[i][k][1], stream=streams[i])
+            cams = [threading.Thread(target=stage, args=(i,)) for i in range(n)]
+            for t in cams:
+                t.start()
+            for t in cams:
+                t.join()
+            batch.process([True] * n)
+            batch.results(back=0)
+    finally:
+        stop.set()
+        mon.join()
+    batch.flush()
+    torch.cuda.synchronize()
+    assert seen
+    for i, s in enumerate(ss):
+        alone = L.System(K, cfg)
+        alone.set_pose(fr[i][0][2])
+        for d, c, _ in fr[i]:
+            alone.process_images(H.cuda(d), H.cuda(c))
+        torch.cuda.synchronize()
+        assert np.array_equal(s.get_camera_pose(), alone.get_camera_pose())
+        for x, y in zip(H.sort_blocks(*s.export()), H.sort_blocks(*alone.export())):
+            assert np.array_equal(x, y)
+    batch.close()
