@@ -222,7 +222,9 @@ struct MarchView {
 constexpr int kRayThreads = 64;
 constexpr int kMaxMarch = 1 << 16;  // safety bound; the march advances >= 1 voxel per step
 
-template <int LAYOUT>
+// RGB: also write the hits' voxel colours (a separate instantiation: the
+// colour pointer kept live across the march costs the plain raycast spills).
+template <int LAYOUT, bool RGB>
 __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionView *__restrict__ svs, float4 *vmap_ext,
                                                                   long long vmap_pitch, int tw, uint8_t *rgb_ext,
                                                                   long long rgb_pitch) {
@@ -249,8 +251,10 @@ __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionV
     *out = make_float4(qnan, qnan, qnan, qnan);
     // colour (raycast_with_colour, ray_tracing.cu:478-564): white unless a hit's
     // nearest voxel has been observed
-    uint8_t *rgb_px = rgb_ext ? rgb_ext + y * rgb_pitch + (long long)x * 3 : nullptr;
-    if (rgb_px) rgb_px[0] = rgb_px[1] = rgb_px[2] = 255;
+    if (RGB) {
+        uint8_t *px = rgb_ext + y * rgb_pitch + (long long)x * 3;
+        px[0] = px[1] = px[2] = 255;
+    }
 
     const int cx = __float2int_rd((float)x / 8), cy = __float2int_rd((float)y / 8);
     if (cx >= sv.zr_w || cy >= sv.zr_h) return;
@@ -301,7 +305,7 @@ __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionV
     if (found) {
         const float3 c = Tcw.apply(r.x * sv.voxel, r.y * sv.voxel, r.z * sv.voxel);
         *out = make_float4(c.x, c.y, c.z, 1.0f);
-        if (rgb_px) {  // read_colour (ray_tracing.cu:427-441): the voxel ToVector3i(pt)
+        if (RGB) {  // read_colour (ray_tracing.cu:427-441): the voxel ToVector3i(pt)
             const int vx = floor_ref(r.x), vy = floor_ref(r.y), vz = floor_ref(r.z);
             const int id = bc.get(mv, voxel_to_block(vx), voxel_to_block(vy), voxel_to_block(vz));
             if (id >= 0) {
@@ -310,9 +314,10 @@ __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionV
                 sdf_at<LAYOUT>(mv, i, observed);
                 if (observed) {
                     const uchar4 col = sv.vox_rgb[i];
-                    rgb_px[0] = col.x;
-                    rgb_px[1] = col.y;
-                    rgb_px[2] = col.z;
+                    uint8_t *px = rgb_ext + y * rgb_pitch + (long long)x * 3;
+                    px[0] = col.x;
+                    px[1] = col.y;
+                    px[2] = col.z;
                 }
             }
         }
@@ -394,12 +399,24 @@ void launch_march(const SessionView *d_sv, int nslots, const Extent &ex, float4 
     const int tw = ray_tile_width(ex), th = kRayThreads / tw;
     // every slot's tiles fit: a smaller frame has fewer tiles per row and per column
     const dim3 g(((ex.w + tw - 1) / tw) * ((ex.h + th - 1) / th), nslots);
+    if (rgb_ext) {
+        if (layouts[GBF_VOXEL_REF])
+            raycast_kernel<GBF_VOXEL_REF, true><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, rgb_ext,
+                                                                           rgb_pitch);
+        if (layouts[GBF_VOXEL_HALF])
+            raycast_kernel<GBF_VOXEL_HALF, true><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, rgb_ext,
+                                                                            rgb_pitch);
+        if (layouts[GBF_VOXEL_SNORM])
+            raycast_kernel<GBF_VOXEL_SNORM, true><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, rgb_ext,
+                                                                             rgb_pitch);
+        return;
+    }
     if (layouts[GBF_VOXEL_REF])
-        raycast_kernel<GBF_VOXEL_REF><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, rgb_ext, rgb_pitch);
+        raycast_kernel<GBF_VOXEL_REF, false><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, nullptr, 0);
     if (layouts[GBF_VOXEL_HALF])
-        raycast_kernel<GBF_VOXEL_HALF><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, rgb_ext, rgb_pitch);
+        raycast_kernel<GBF_VOXEL_HALF, false><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, nullptr, 0);
     if (layouts[GBF_VOXEL_SNORM])
-        raycast_kernel<GBF_VOXEL_SNORM><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, rgb_ext, rgb_pitch);
+        raycast_kernel<GBF_VOXEL_SNORM, false><<<g, kRayThreads, 0, st>>>(d_sv, vmap_ext, vmap_pitch, tw, nullptr, 0);
 }
 
 void launch_nmap_of(const float4 *vmap, long long vmap_pitch, float4 *nmap, long long nmap_pitch, int w, int h,
