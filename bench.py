@@ -153,30 +153,49 @@ def render_frames(L, K, seeds, n_frames):
 
 
 class ClockSampler:
-    """nvidia-smi SM clocks and throttle reasons during the timed region."""
+    """nvidia-smi SM clocks and throttle reasons during the timed region.
+
+    The sampler starts before the region and waits (at most 5 s) for its first
+    reading, so that the region is covered from its start; every line is
+    stamped when it arrives, and the summary keeps the lines stamped between
+    start() and stop() (the nearest one when the region is shorter than the
+    sampling period)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 100
 
     def __init__(self, gpu_index: int):
         self.idx = gpu_index
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list[tuple[float, str]] = []
+        self.first = threading.Event()
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=5.0)
         except Exception:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+            self.first.set()
+
+    def start(self):
+        self.t0 = time.perf_counter()
+
+    def stop(self):
+        self.t1 = time.perf_counter()
+        # one more period, so that a reading taken just before stop() has arrived
+        time.sleep(self.PERIOD_MS / 1e3)
 
     def __exit__(self, *a):
         if self.proc:
@@ -187,9 +206,15 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        t0 = self.t0 if self.t0 is not None else float("-inf")
+        t1 = self.t1 if self.t1 is not None else float("inf")
+        inside = [ln for t, ln in self.lines if t0 <= t <= t1 + self.PERIOD_MS / 1e3]
+        if not inside and self.lines:
+            mid = 0.5 * (self.t0 + self.t1) if self.t0 is not None and self.t1 is not None else self.lines[-1][0]
+            inside = [min(self.lines, key=lambda tl: abs(tl[0] - mid))[1]]
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in inside:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -204,8 +229,11 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"], "samples": 0}
         load = [x for x in sm if x > 0.5 * max(sm)] or sm
-        return {"sm_mhz": statistics.median(load), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(load), "sm_max_mhz": mx, "reasons": sorted(reasons),
+               "samples": len(sm), "period_ms": self.PERIOD_MS}
+        if self.t0 is not None and self.t1 is not None:
+            out["region_s"] = round(self.t1 - self.t0, 3)
+        return out
 
 
 # DRAM bytes one pixel-iteration of the ICP + photometric reduction moves, from
@@ -508,6 +536,7 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
+        clocks.start()
         t_wall = time.perf_counter()
         for k in range(steps):
             ev[k][0].record(stream)
@@ -515,6 +544,7 @@ def run_ours(args):
             ev[k][1].record(stream)
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
+        clocks.stop()
     if world > 1:
         dist.barrier()
     tick_ms = [a.elapsed_time(b) for a, b in ev]
@@ -744,11 +774,14 @@ def run_mixed(args):
         tick(k)
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    for k in range(steps):
-        ev[k][0].record(stream)
-        tick(warm + k)
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        clocks.start()
+        for k in range(steps):
+            ev[k][0].record(stream)
+            tick(warm + k)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        clocks.stop()
     tick_ms = sorted(a.elapsed_time(b) for a, b in ev)
     total_ms = ev[0][0].elapsed_time(ev[-1][1])
     value = S * steps / (total_ms / 1e3)
@@ -778,7 +811,7 @@ def run_mixed(args):
         "config": {"workload": f"{S} sessions per tick: resolutions {['%dx%d' % s for s in MIXED_SIZES]} and voxels "
                                f"{[f'{v * 1000:.0f} mm' for v in MIXED_VOXELS]} cycled over the sessions",
                    "voxel_layout": LAYOUTS[LAYOUT][1], "launch_shape": shape},
-        "latency_ms": {"p50": p(0.5), "p99": p(0.99)},
+        "latency_ms": {"p50": p(0.5), "p99": p(0.99)}, "clocks": clocks.summary(),
         "plain": {"value": plain, "unit": UNIT, "frames": S * per}, "served_vs_plain": value / plain,
     }), flush=True)
 
