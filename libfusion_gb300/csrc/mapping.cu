@@ -343,7 +343,8 @@ void launch_visible_frustum(const SessionView *d_sv, int nslots, const Extent &e
 void launch_integrate(const SessionView *d_sv, int nslots, const Extent &ex, int mode, const int *layouts,
                       cudaStream_t st) {
     if (mode != 1) fuse_prep_kernel<<<dim3((ex.w * ex.h + 255) / 256, nslots), 256, 0, st>>>(d_sv, mode);
-    // one CTA per visible block, grid-stride; 8 resident CTAs of 256 threads per SM
+    // one CTA per visible block, grid-stride over 8 CTAs per SM per session (16 of
+    // 128 threads are resident per SM)
     const int gi = 152 * 8;
     if (layouts[GBF_VOXEL_REF]) integrate_kernel<GBF_VOXEL_REF><<<dim3(gi, nslots), kIntThreads, 0, st>>>(d_sv, mode);
     if (layouts[GBF_VOXEL_HALF]) integrate_kernel<GBF_VOXEL_HALF><<<dim3(gi, nslots), kIntThreads, 0, st>>>(d_sv, mode);
