@@ -28,6 +28,7 @@ def _fused(L, layout):
     cfg = H.small_config(L, layout)
     m = L.DenseMapping(K, cfg)
     o64 = O.OracleMap(O.config_from(cfg), O.intrinsics_from(K), "f64")
+    o32 = O.OracleMap(O.config_from(cfg), O.intrinsics_from(K), "f32")
     fr = O.OracleFrame(O.config_from(cfg), O.intrinsics_from(K))
     frames = H.frames(L, K, N_FUSE, step=1)
     for d, c, T in frames:
@@ -36,7 +37,8 @@ def _fused(L, layout):
         n0 = fr.get(1, 0)
         m.update(H.cuda(dm), H.cuda(c), T, normal=H.cuda(n0))
         o64.fuse(dm, c, T, nmap=n0)
-    _FUSED[layout] = (K, cfg, m, o64, frames[-1][2])
+        o32.fuse(dm, c, T, nmap=n0)
+    _FUSED[layout] = (K, cfg, m, o64, frames[-1][2], o32)
     return _FUSED[layout]
 
 
@@ -52,13 +54,29 @@ def _common(gmap, omap):
 
 @pytest.mark.parametrize("layout", [0, 1, 2])
 def test_tsdf_error_vs_fp64_oracle(gbf, layout):
-    K, cfg, m, o64, _ = _fused(gbf, layout)
-    gs, gw, os_, ow = _common(m.export(), o64.export())
+    K, cfg, m, o64, _, o32 = _fused(gbf, layout)
+    gmap = m.export()
+    gs, gw, os_, ow = _common(gmap, o64.export())
     both = (gw > 0) & (ow > 0)
     err = np.abs(gs[both] - os_[both])   # sdf is stored in units of the truncation distance
     p999 = float(np.quantile(err, 0.999))
+    # the same error split in two: the kernels and the layout's storage against
+    # the FP32 oracle (the reference's arithmetic in the layout's storage), and
+    # that FP32 arithmetic itself against FP64
+    gs2, gw2, fs, fw = _common(gmap, o32.export())
+    impl = np.abs(gs2[(gw2 > 0) & (fw > 0)] - fs[(gw2 > 0) & (fw > 0)])
+    fs3, fw3, os3, ow3 = _common(o32.export(), o64.export())
+    arith = np.abs(fs3[(fw3 > 0) & (ow3 > 0)] - os3[(fw3 > 0) & (ow3 > 0)])
     print(f"layout {layout}: voxels {both.sum()}, TSDF |err|/tau max {err.max():.2e} p99.9 {p999:.2e} "
-          f"mean {err.mean():.2e}")
+          f"mean {err.mean():.2e}; GPU vs FP32 oracle max {impl.max():.2e}; FP32 oracle vs FP64 max "
+          f"{arith.max():.2e} p99.9 {np.quantile(arith, 0.999):.2e}, above 1e-3: GPU {np.sum(err > 1e-3)} "
+          f"FP32 oracle {np.sum(arith > 1e-3)}")
+    # The maximum comes from the reference's FP32 arithmetic, not from this
+    # implementation: the FP32 oracle is as far from FP64 at its worst voxel, and
+    # the GPU stays within a few storage steps of the FP32 oracle everywhere
+    # (sinf rounds differently in CUDA and libm; HALF's fp16 step near 1 is 4.9e-4).
+    assert impl.max() <= (4e-3 if layout == 1 else 5e-4)
+    assert abs(err.max() - arith.max()) <= impl.max()
     # FP32 and FP64 can pick a different depth pixel for a voxel on a pixel
     # boundary, so the bound is on the distribution.  REF (int16 sdf, 3e-5
     # quantum, truncating) and SNORM (the same quantum, rounded to nearest):
@@ -79,7 +97,7 @@ def test_raycast_depth_vs_fp64_oracle(gbf, layout):
     counted and bounded separately."""
     import torch
     L = gbf
-    K, cfg, m, o64, T = _fused(L, layout)
+    K, cfg, m, o64, T, _ = _fused(L, layout)
     vm = torch.full((K.height, K.width, 4), float("nan"), device="cuda")
     m.raycast(vm, T)
     g = vm.cpu().numpy()
@@ -110,7 +128,7 @@ def test_mesh_chamfer_vs_fp64_oracle(gbf, layout):
     import torch
     spatial = pytest.importorskip("scipy.spatial")
     L = gbf
-    K, cfg, m, o64, _ = _fused(L, layout)
+    K, cfg, m, o64, _, _ = _fused(L, layout)
     ov, _ = o64.mesh(0, 1 << 22)
     cap = len(ov) + (1 << 16)
     vtx = torch.zeros((cap, 3, 3), dtype=torch.float32, device="cuda")
