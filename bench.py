@@ -240,6 +240,12 @@ class ClockSampler:
 # one ncu capture of a level-0 launch over 4 sessions (100.83 MB for 1,228,800
 # pixel-iterations; profiles/gn_reduce_kernel_4x640x480.md): the roofline's traffic
 REDUCE_DRAM_BYTES_PER_PIXEL_ITER = 100.36224e6 / 1228800
+# DRAM bytes per raycast pixel, from one ncu capture of the HALF raycast over 4
+# sessions (66.30 MB read + 4.26 MB written for 4 x 307,200 pixels;
+# profiles/raycast_kernel_4x640x480.md), and its issue-active fraction there.
+# The bytes depend on the maps the rays cross, so scaling by pixels is an estimate.
+RAYCAST_DRAM_BYTES_PER_PIXEL = (66.297856e6 + 4.257280e6) / (4 * 307200)
+RAYCAST_ISSUE_ACTIVE = 0.761
 
 
 def measured_peaks():
@@ -590,11 +596,21 @@ def run_ours(args):
                                  "times this run's pixel-iterations per launch" if traffic is not None else None,
                 "work_per_step": {"pixel_iterations": pix_iter, "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
                 "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream",
-                "why_this_kernel": "the raycast's march (the other ~35% of launch time, profiles/"
+                "why_this_kernel": "the raycast (37% of launch time against the reduction's 35%, profiles/"
                                    "launches_fusion_tick_64x640x480.md) is bound by instruction issue, not HBM "
-                                   "(76% issue active, DRAM 2.7%: profiles/raycast_kernel_4x640x480.md); the "
-                                   "HBM roofline is given for the larger memory-bound phase",
+                                   "(76% issue active, DRAM 2.7%: profiles/raycast_kernel_4x640x480.md), so its "
+                                   "figures are under 'march'; the HBM roofline is given for the memory-bound phase",
                 "march_ms_per_step": phases["march"]}
+    px_step = sum(s.K.width * s.K.height for s in sessions)
+    march_bytes = RAYCAST_DRAM_BYTES_PER_PIXEL * px_step
+    roofline["march"] = {
+        "kernel": "raycast_kernel", "bound": "issue", "ms_per_step": phases["march"],
+        "issue_active_ncu": RAYCAST_ISSUE_ACTIVE,
+        "dram_bytes_per_step_est": march_bytes,
+        "dram_gbs_est": march_bytes / (phases["march"] / 1e3) / 1e9,
+        "dram_frac_est": march_bytes / (phases["march"] / 1e3) / 1e9 / peak,
+        "basis": "DRAM bytes per pixel from one ncu capture of the raycast at 4 sessions, times this "
+                 "run's raycast pixels, over the phase's CUDA-event time; issue activity from the same capture"}
 
     # ---- end to end through the public API with host buffers (pinned): the same
     # frames as the timed ticks, after the same warm-up frames (untimed).  Each
