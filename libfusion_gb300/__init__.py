@@ -416,9 +416,12 @@ class FusionBatch:
         return int(n.value)
 
     def close(self) -> None:
+        """Destroy the batch and let go of the sessions in its slots (they stay
+        usable on their own)."""
         if self._h:
             call("gbf_batch_destroy", self._h)
             self._h = C.c_void_p()
+        self.slots = [None] * len(self.slots)
 
     def __del__(self):
         try:
