@@ -238,11 +238,11 @@ class ClockSampler:
 
 # DRAM bytes one pixel-iteration of the ICP + photometric reduction moves, from
 # one ncu capture of a level-0 launch over 4 sessions (100.83 MB for 1,228,800
-# pixel-iterations; profiles/gn_reduce_kernel_4x640x480.md): the roofline's traffic
+# pixel-iterations, dram__bytes_read.sum + dram__bytes_write.sum): the roofline's traffic
 REDUCE_DRAM_BYTES_PER_PIXEL_ITER = 100.36224e6 / 1228800
 # DRAM bytes per raycast pixel, from one ncu capture of the HALF raycast over 4
 # sessions (66.30 MB read + 4.26 MB written for 4 x 307,200 pixels;
-# profiles/raycast_kernel_4x640x480.md), and its issue-active fraction there.
+# same counters), and its issue-active fraction there.
 # The bytes depend on the maps the rays cross, so scaling by pixels is an estimate.
 RAYCAST_DRAM_BYTES_PER_PIXEL = (66.297856e6 + 4.257280e6) / (4 * 307200)
 RAYCAST_ISSUE_ACTIVE = 0.761
@@ -592,13 +592,13 @@ def run_ours(args):
                 "launches_per_step": n_launch, "peak_source": f"{peak_kind} hbm_gbs",
                 "algorithmic_bytes_per_launch": bytes_step / n_launch, "algorithmic_bytes_per_step": bytes_step,
                 "traffic_basis": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0 launch at 4 "
-                                 "sessions (profiles/gn_reduce_kernel_4x640x480.md): 81.7 B per pixel-iteration, "
+                                 "sessions: 81.7 B per pixel-iteration, "
                                  "times this run's pixel-iterations per launch" if traffic is not None else None,
                 "work_per_step": {"pixel_iterations": pix_iter, "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
                 "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream",
-                "why_this_kernel": "the raycast (37% of launch time against the reduction's 35%, profiles/"
-                                   "launches_fusion_tick_64x640x480.md) is bound by instruction issue, not HBM "
-                                   "(76% issue active, DRAM 2.7%: profiles/raycast_kernel_4x640x480.md), so its "
+                "why_this_kernel": "the raycast (37% of launch time against the reduction's 35% in an ncu "
+                                   "launch list of the 64-session tick) is bound by instruction issue, not HBM "
+                                   "(76% issue active, DRAM 2.7% in its ncu capture at 4 sessions), so its "
                                    "figures are under 'march'; the HBM roofline is given for the memory-bound phase",
                 "march_ms_per_step": phases["march"]}
     px_step = sum(s.K.width * s.K.height for s in sessions)

@@ -243,8 +243,8 @@ GBF_API gbf_status gbf_reduce(gbf_session *s, int32_t level, const double T[16],
  * rows; vertex / normal maps float4 per pixel, intensities and gradients float).
  * The vertex and normal maps and the reference intensity start on 16-byte
  * boundaries, the other images on 4-byte boundaries (GBF_ERR_INVALID_ARG
- * otherwise); the reference intensity is read in 16-byte chunks, so up to 12
- * bytes past its last pixel, which a cudaMalloc'd image always has. */
+ * otherwise); nothing past an image's last pixel is read, so the images may sit
+ * back to back in one buffer. */
 typedef struct gbf_reduce_inputs {
     int32_t width, height;
     float fx, fy, cx, cy;
@@ -253,14 +253,15 @@ typedef struct gbf_reduce_inputs {
     float dist_thresh, angle_thresh;
 } gbf_reduce_inputs;
 /* No counterpart in the reference: the same 58 sums as gbf_reduce, for callers
- * that cannot allocate device memory (inside CUDA graph capture, allocation-free
- * real-time loops, frameworks that own all device memory).  Needs no session and
- * calls no cudaMalloc / cudaFree: its scratch (per-CTA partials + a ticket) is a
- * fixed 512 KB array in the library that every GPU loading the library keeps
- * until exit.  Images up to 2,097,152 pixels (larger ones return
- * GBF_ERR_CAPACITY).  out_dev: 58 doubles of device memory, written on `stream`.
- * The first call on a device looks the array's address up (make it before any
- * stream capture); calls that overlap on the GPU share the array and race. */
+ * that cannot allocate device memory -- real-time loops that forbid allocation
+ * once they run, and frameworks that hand out all device memory through their
+ * own allocator.  Needs no session and calls no cudaMalloc / cudaFree: its
+ * scratch (per-CTA partials + a ticket) is a fixed 512 KB array in the library
+ * that every GPU loading the library keeps until exit.  Images up to 2,097,152
+ * pixels (larger ones return GBF_ERR_CAPACITY).  out_dev: 58 doubles of device
+ * memory, 8-byte aligned, written on `stream`.  The first call on a device
+ * looks the array's address up (make it before any stream capture); calls that
+ * overlap on the GPU share the array and race. */
 GBF_API gbf_status gbf_reduce_noalloc(const gbf_reduce_inputs *in, const double T[16], float stddev,
                                       double *out_dev, void *stream);
 /* Coarse-to-fine Gauss-Newton between the reference and current sets. Synchronises. */
@@ -355,6 +356,9 @@ GBF_API gbf_status gbf_zrange(gbf_session *s, float *out_host, int64_t max_cells
 
 /* ---- batch: many sessions per launch ----------------------------------------- */
 GBF_API gbf_status gbf_batch_create(int32_t max_sessions, gbf_batch **out);
+/* Destroying a batch frees it: no other gbf_batch_* call on it may be pending
+ * on another thread, or start, once gbf_batch_destroy begins (the batch's lock
+ * cannot outlive the batch). */
 GBF_API gbf_status gbf_batch_destroy(gbf_batch *b);
 GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s);
 /* One frame for every slot with active[slot] != 0, from each session's staging

@@ -970,7 +970,10 @@ static void batch_invalidate(gbf_batch *b) {
 
 GBF_API gbf_status gbf_batch_destroy(gbf_batch *b) {
     if (!b) return GBF_OK;
-    std::unique_lock<std::mutex> lock(b->mu);  // a call in flight on another thread ends first
+    // The caller guarantees that no other gbf_batch_* call on b is pending or
+    // starts once destroy begins; taking the lock only orders this thread
+    // after a call that returned on another thread.
+    std::unique_lock<std::mutex> lock(b->mu);
     if (b->d_views_b) batch_flush(b, nullptr);  // the sessions outlive the batch: fuse what is owed
     cudaDeviceSynchronize();
     batch_invalidate(b);

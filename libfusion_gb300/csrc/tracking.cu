@@ -403,13 +403,18 @@ __device__ __forceinline__ void cta_partial(ReduceSmem &sm, const SessionView &s
                     cp_async16(&s_n[c], gn + c);
                 }
             }
-        } else {  // intensities in 16-byte chunks of 4 pixels (the last may run up to
-                  // 3 floats past the image, inside its 256-byte-rounded allocation)
+        } else {  // intensities in 16-byte chunks of 4 pixels; a chunk that would run
+                  // past the image's last pixel is copied pixel by pixel instead, so
+                  // nothing past the image is read
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
                 const int q = ln + 32 * j;  // 8 runs of the pair's pixels x 8 chunks
                 const int c = (q >> 3) * kHalfThreads + 32 * pair + 4 * (q & 7);
-                if (c < n) cp_async16(&s_i[c], gi + c);
+                if (c + 4 <= n) {
+                    cp_async16(&s_i[c], gi + c);
+                } else {
+                    for (int k = c; k < n; ++k) s_i[k] = gi[k];
+                }
             }
         }
         asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
@@ -788,10 +793,11 @@ void launch_slot_results(const SessionView *d_sv, int nslots, gbf_slot_result *o
 // ============================================================================
 // Allocation-free ICP + photometric reduction.
 //
-// Some callers cannot allocate device memory at all: code running while a CUDA
-// graph is being captured (cudaMalloc is not capturable), real-time loops that
-// forbid allocation after start-up, and host frameworks that hand out every
-// byte of device memory through their own allocator.  For them this entry
+// Some callers cannot allocate device memory at all: real-time camera loops
+// that forbid allocation once they run (a cudaMalloc can block for
+// milliseconds and synchronise the device), and host frameworks that hand out
+// every byte of device memory through their own allocator, so that a library
+// allocating behind their back would fail or break their accounting.  For them this entry
 // point reduces one pyramid level of caller-owned images with no session and no
 // cudaMalloc / cudaFree: its per-CTA partial sums and its last-CTA ticket live
 // in the file-scope array below, which every GPU that loads the library keeps
@@ -868,6 +874,8 @@ extern "C" GBF_API gbf_status gbf_reduce_noalloc(const gbf_reduce_inputs *in, co
         !aligned(in->cur_didx, 4) || !aligned(in->cur_didy, 4))
         return set_error(GBF_ERR_INVALID_ARG,
                          "gbf_reduce_noalloc: vertex, normal and reference intensity images must be 16-byte aligned");
+    if (!aligned(out_dev, 8))  // written as doubles
+        return set_error(GBF_ERR_INVALID_ARG, "gbf_reduce_noalloc: out_dev must be 8-byte aligned");
     const long long pixels = (long long)in->width * in->height;
     if (pixels > (long long)kStaticReduceCtas * kReduceThreads * kReducePixelsPerThread)
         return set_error(GBF_ERR_CAPACITY, "gbf_reduce_noalloc: at most 2,097,152 pixels per image");

@@ -9,9 +9,10 @@ recorded as SHA-256 digests of their canonical JSON text, so the fixture pins
 them without carrying a copy.  Needs the reference tree, so it runs here, not
 on the GPU machine; the committed JSON is what the tests read.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]  (default: $LIBFUSION_REFERENCE)
 """
 import hashlib
+import os
 import json
 import subprocess
 import sys
@@ -25,7 +26,7 @@ def digest(obj) -> str:
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LIBFUSION_REFERENCE", "/root/reference")
     exe = subprocess.run([str(ROOT / "oracle/ref_pin/build_ref.sh"), ref], check=True, capture_output=True,
                          text=True).stdout.strip().splitlines()[-1]
     data = json.loads(subprocess.run([exe], check=True, capture_output=True, text=True).stdout)

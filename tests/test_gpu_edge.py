@@ -142,3 +142,31 @@ def test_misaligned_images_are_rejected(gbf):
     d, c, T2 = H.frames(L, K, 1)[0]
     m.update(H.cuda(H.depth_m(d)), H.cuda(c), T2)
     assert m.stats().allocated_blocks > 0
+
+
+def test_positions_dropped_by_a_full_pool_allocate_after_pruning(gbf):
+    """A block that found the pool full keeps its claimed table slot with no
+    block behind it; that can only matter once room is made, and room is only
+    made by deleting or pruning blocks, which rebuild the table from the
+    allocated blocks alone.  So the next frame allocates positions the full
+    pool had dropped."""
+    L = gbf
+    K = H.intrinsics(L)
+    m = L.DenseMapping(K, H.small_config(L, 0, num_blocks=64))
+    d, c, T = H.frames(L, K, 1)[0]
+    depth, rgb = H.cuda(H.depth_m(d)), H.cuda(c)
+    m.update(depth, rgb, T)
+    first = {tuple(x) for x in m.export()[0]}
+    assert len(first) == 64 and m.stats().status & L.FLAG_POOL_EXHAUSTED
+    gone = np.array(sorted(first)[:32], np.int32)
+    assert m.delete_blocks(gone) == 32
+    assert m.stats().allocated_blocks == 32
+    m.update(depth, rgb, T)
+    second = {tuple(x) for x in m.export()[0]}
+    assert len(second) == 64
+    assert second - first, "only positions the pool had held before were allocated again"
+    # every block pruned (radius 0 around the camera): the pool refills from the frame
+    assert m.prune(center=T[:3, 3], radius=0.0) == 64
+    assert m.stats().allocated_blocks == 0
+    m.update(depth, rgb, T)
+    assert m.stats().allocated_blocks == 64

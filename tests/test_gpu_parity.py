@@ -397,3 +397,33 @@ def test_raycast_maps_bit_exact(gbf, layout):
     vm2 = torch.full((K.height, K.width, 4), float("nan"), device="cuda")
     m.raycast(vm2, T)
     assert np.array_equal(np.nan_to_num(vm2.cpu().numpy(), nan=7.0), np.nan_to_num(g, nan=7.0))
+
+
+def test_post_raycast_pyramid_bit_exact(gbf):
+    """DeviceImage::resize_device_map (src/tracking/device_image.cpp:188-199):
+    after a frame, the next frame's reference vertex map is the raycast at the
+    tracked pose (level 0), levels 1-2 its 2x2 means, and every level's normals
+    recomputed from it.  Level 0 is checked against a raycast of the same map
+    at the same pose, levels 1-2 and all normal maps bit for bit against the
+    oracle's pyramid built from that level 0."""
+    import oracle as O
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 0, bilateral=0)
+    fr = H.frames(L, K, 3)
+    s = L.System(K, cfg)
+    s.set_pose(fr[0][2])
+    for d, c, T in fr:
+        s.process_images(H.cuda(d), H.cuda(c))
+    v0 = s.get_image(1, 0, 0).cpu().numpy()
+    vm = torch.empty((K.height, K.width, 4), dtype=torch.float32, device="cuda")
+    s.raycast(vm, s.get_camera_pose())
+    assert np.array_equal(v0, vm.cpu().numpy(), equal_nan=True), "level 0 is not the raycast"
+    assert np.isfinite(v0[..., 2]).mean() > 0.5
+    of = O.OracleFrame(O.config_from(cfg), O.intrinsics_from(K))
+    of.set_vmap(v0)
+    for lvl in range(3):
+        for kind in (0, 1):
+            g = s.get_image(1, kind, lvl).cpu().numpy()
+            assert np.array_equal(g, of.get(kind, lvl), equal_nan=True), (lvl, kind)
