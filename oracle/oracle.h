@@ -16,7 +16,10 @@
  *
  * Parity pins: the marching-cubes tables, computeHash and the coordinate
  * converters are checked against outputs of the reference's own source
- * compiled here (tests/golden/make_golden.py).  The kernels' third-party
+ * compiled here (tests/golden/make_golden.py); the integration, z-range,
+ * raycast, ICP-row and photometric-row bodies against outputs of the
+ * reference's own kernels, compiled from its sources and run on a GPU
+ * (tests/golden/make_kernel_golden.py, tests/test_ref_kernel_pins.py).  The kernels' third-party
  * steps (OpenCV bilateral / resize / pyrDown / cvtColor, Sophus SE(3), Eigen
  * LDLT) have no reference implementation available and are restated from
  * their documented definitions: parity of those steps is unpinned.
