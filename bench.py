@@ -40,7 +40,8 @@ VOXELS = (0.005, 0.006, 0.008, 0.01)  # served sessions draw voxel sizes of 5-10
 LAYOUTS = {"half": (1, "fp16 sdf + binary16 weight + rgba8 (8 B/voxel)"),
            "snorm": (2, "int16 sdf (rounded) + binary16 weight + rgba8 (8 B/voxel)"),
            "ref": (0, "int16 sdf (truncated) + f32 weight + rgba8 (12 B/voxel)")}
-LAYOUT = "half"
+LAYOUT = "snorm"  # the 8-byte layout within the 1e-3 x truncation TSDF error goal (HALF's fp16 step is not)
+PREC_FRAMES = 20  # frames of the precision check (tracking loop and mapping at ground-truth poses)
 
 
 def parse():
@@ -58,10 +59,14 @@ def parse():
     ap.add_argument("--tune-ticks", type=int, default=6, help="timed ticks per tuner candidate")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--serve-ticks", type=int, default=120, help="ticks of the churn (arrival / eviction) run")
-    ap.add_argument("--layout", default="half", choices=sorted(LAYOUTS), help="voxel storage of every session")
-    ap.add_argument("--workload", default="served", choices=["served", "mixed"],
+    ap.add_argument("--layout", default="snorm", choices=sorted(LAYOUTS), help="voxel storage of every session")
+    ap.add_argument("--precision-frames", type=int, default=PREC_FRAMES,
+                    help="frames of the precision check against the FP64 oracle (0: skip)")
+    ap.add_argument("--workload", default="served", choices=["served", "mixed", "scale"],
                     help="mixed: sessions of three resolutions and three voxel sizes in one batch "
-                         "(served vs plain only; prints its own line)")
+                         "(served vs plain only; prints its own line); scale: the large-map "
+                         "configuration as one plain session, phase by phase")
+    ap.add_argument("--scale-frames", type=int, default=2000, help="frames of the scale workload")
     return ap.parse_args()
 
 
@@ -373,6 +378,93 @@ def cpu_baseline(L, K, seconds: float, warmup: int):
             "fp64_oracle": {"value": len(t64) / sum(t64), "unit": UNIT, "cores": threads,
                             "sample": cpu_sample_text(len(t64), n_mix, threads).replace("FP32", "FP64")
                             + f", {sum(t64):.1f} s; the error reference, timed for the record"}}
+
+
+def precision_gpu(L, K, cfg, fr):
+    """The GPU side of the precision check on one session's frames `fr`
+    (depth u16, rgb, ground-truth pose): the tracking loop (System, the plain
+    path, whose results the served batch reproduces bit for bit), and the
+    normal-weighted mapping at the ground-truth poses with each frame's own
+    normal map, raycast at the last pose."""
+    import torch
+    cu = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    s = L.System(K, cfg)
+    s.set_pose(fr[0][2])
+    poses = []
+    for d, c, _ in fr:
+        s.process_images(cu(d), cu(c))
+        poses.append(s.get_camera_pose())
+    s.close()
+    t, m, nmaps = L.DenseTracking(K, cfg), L.DenseMapping(K, cfg), []
+    for d, c, T in fr:
+        dm = cu(d.astype(np.float32) * np.float32(0.001))
+        t.set_current(dm, cu(c))
+        n = t.get_image(0, 1, 0)  # the frame's level-0 normals (from the filtered depth, as System fuses)
+        m.update(dm, cu(c), T, normal=n)
+        nmaps.append(n.cpu().numpy())
+    vm = torch.full((K.height, K.width, 4), float("nan"), dtype=torch.float32, device="cuda")
+    m.raycast(vm, fr[-1][2])
+    out = {"poses": np.array(poses), "map": m.export(), "vmap": vm.cpu().numpy(), "nmaps": nmaps}
+    m.close()
+    t.close()
+    return out
+
+
+def precision_check(L, K, cfg, fr, g, threads):
+    """CPU leg: the FP64 oracle (double arithmetic, unquantised voxels) on the
+    same frames, as the checker of the GPU results `g`: pose drift of the
+    tracking loop, TSDF error of the ground-truth-pose map (sdf in units of
+    the truncation distance, voxels observed in both maps), raycast depth of
+    that map at the last pose (rays on the same surface, |dz| < truncation),
+    and the tracking loop's trajectory error against the ground truth."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    O.build()
+    oc, ok = O.config_from(cfg, threads=threads), O.intrinsics_from(K)
+    t0 = time.perf_counter()
+    osys = O.OracleSystem(oc, ok, "f64")
+    osys.set_pose(fr[0][2])
+    op = []
+    for d, c, _ in fr:
+        osys.process(d, c)
+        op.append(osys.pose())
+    op = np.array(op)
+    gp = g["poses"]
+    om = O.OracleMap(oc, ok, "f64")
+    for (d, c, T), n in zip(fr, g["nmaps"]):
+        om.fuse(d.astype(np.float32) * np.float32(0.001), c, T, nmap=n)
+    gc, gs, gw, _ = g["map"]
+    oc_, os_, ow, _ = om.export()
+    key = lambda a: a[:, 0].astype(np.int64) * (1 << 42) + a[:, 1].astype(np.int64) * (1 << 21) + a[:, 2]
+    gk, okk = key(gc.astype(np.int64) + (1 << 20)), key(oc_.astype(np.int64) + (1 << 20))
+    common, gi, oi = np.intersect1d(gk, okk, return_indices=True)
+    gs, gw, os_, ow = gs[gi], gw[gi], os_[oi], ow[oi]
+    both = (gw > 0) & (ow > 0)
+    err = np.abs(gs[both] - os_[both]).astype(np.float64)
+    ov = om.raycast(fr[-1][2])
+    gv = g["vmap"]
+    gh, oh = ~np.isnan(gv[..., 2]), ~np.isnan(ov[..., 2])
+    dz = np.abs(gv[..., 2][gh & oh] - ov[..., 2][gh & oh]).astype(np.float64)
+    same = dz < cfg.truncation
+    truth = np.array([T for _, _, T in fr])
+    ate = np.sqrt(np.mean(np.sum((gp[:, :3, 3] - truth[:, :3, 3]) ** 2, axis=1)))
+    return {
+        "reference": "FP64 oracle (double arithmetic, unquantised voxels) on the host cores",
+        "session": f"{len(fr)} frames of served session 0 (640x480, voxel {cfg.voxel_size * 1e3:.0f} mm, "
+                   f"truncation {cfg.truncation * 1e3:.0f} mm, {LAYOUTS[LAYOUT][1]})",
+        "pose_drift_mm": float(np.abs(gp[:, :3, 3] - op[:, :3, 3]).max() * 1e3),
+        "pose_drift_goal_mm": 1.0,
+        "tsdf_err_over_tau": {"p99.9": float(np.quantile(err, 0.999)), "mean": float(err.mean()),
+                              "max": float(err.max()), "voxels": int(both.sum()),
+                              "above_1e-3": int(np.sum(err > 1e-3)), "goal_p99.9": 1e-3,
+                              "basis": "normal-weighted updates at the ground-truth poses, voxels observed in both "
+                                       "maps; sdf is stored in units of the truncation distance"},
+        "raycast_depth_mm": {"same_surface_rms": float(np.sqrt(np.mean(dz[same] ** 2)) * 1e3),
+                             "p99": float(np.quantile(dz[same], 0.99) * 1e3), "rays": int(same.sum()),
+                             "other_surface": int(np.sum(~same)), "hit_masks_differing": int(np.sum(gh != oh))},
+        "ate_vs_ground_truth_mm": float(ate * 1e3),
+        "oracle_seconds": round(time.perf_counter() - t0, 1),
+    }
 
 
 def host_frames(L, K, n, seed=0):
@@ -709,9 +801,16 @@ def run_ours(args):
                     "basis": "camera->world pose of each of the first sessions after the same frame, from the "
                              "pipelined batch of all sessions (e2e leg) and from the plain one-session path"}
 
+    prec_frames = host_frames(L, K, args.precision_frames, seed=replica_seeds(rank, S)[0]) \
+        if args.precision_frames > 0 and rank == 0 else None
+    prec_gpu = precision_gpu(L, K, session_config(L, 0), prec_frames) if prec_frames else None
+
     if rank != 0:
         return
     cpu = cpu_baseline(L, K, args.cpu_seconds, warm)
+    # the CPU leg also runs the FP64 oracle as the checker of the GPU's results
+    precision = precision_check(L, K, session_config(L, 0), prec_frames, prec_gpu, os.cpu_count() or 1) \
+        if prec_gpu else None
     clk = clocks.summary()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warm,
@@ -725,6 +824,7 @@ def run_ours(args):
         "plain": plain, "served_vs_plain": value / plain_fps, "served_vs_plain_results": same_results,
         "serving": serving,
         "phases_ms": {k: v for k, v in phases.items()},
+        "precision": precision,
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": kpt * steps,
         "clocks": clk, "tracking_failures": failed, "sessions_with_errors": bad,
         "wall_s": t_wall,
@@ -841,6 +941,172 @@ def run_mixed(args):
     }), flush=True)
 
 
+# the large-map configuration: 8x8x3 m room, 20 spheres, 12 boxes, figure-eight at 0.5 m/s and 30 fps
+SCALE_SCENE = dict(trajectory=1, room=(8, 8, 3), n_spheres=20, n_boxes=12, radius=2.5, speed=0.5, fps=30, seed=2)
+SCALE_MESH_EVERY = 100
+
+
+def scale_config(L):
+    return L.default_config(voxel_size=0.005, truncation=0.02, zmin_update=0.3, zmax_update=4.0, zmin_raycast=0.3,
+                            zmax_raycast=4.0, num_buckets=1 << 21, num_blocks=1 << 20,
+                            voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3, max_iterations=[10, 5, 3, 3, 3],
+                            w_icp=1.0, w_rgb=0.1, max_probe=1024)
+
+
+def phase_bytes(phase: str, P: int, levels: int, s_v: int, d: dict) -> float | None:
+    """Algorithmic bytes of one frame's phase (the kernels' own reads and
+    writes, each byte once): d holds the frame's work counters."""
+    Pl = [P >> (2 * l) for l in range(levels)]
+    if phase == "ingest":   # u16 depth + rgb8 in; depth, intensity out; pyramids; per level vmap, nmap, gradients
+        return 5 * P + 8 * P + sum(8 * (Pl[l - 1] + Pl[l]) for l in range(1, levels)) + sum(48 * x for x in Pl)
+    if phase == "track":    # reference vmap+nmap+I, current vmap+nmap+I+gradients per pixel-iteration
+        return 80.0 * d["pixel_iterations"]
+    if phase == "alloc_visible":  # depth in; per allocated block its record; the visible list out (lower bound)
+        return 4 * P + 20.0 * d["allocated_blocks"] + 4.0 * d["visible_blocks"]
+    if phase == "integrate":  # voxel read-modify-write of every visible block + depth, normal, colour per pixel
+        return 2.0 * s_v * 512 * d["integrated_blocks"] + 23 * P
+    if phase == "zrange":
+        return 20.0 * d["visible_blocks"] + 8 * (P // 64)
+    if phase == "post":     # vertex maps halved per level, normals recomputed per level
+        return sum(16 * (Pl[l - 1] + Pl[l]) for l in range(1, levels)) + sum(32 * x for x in Pl)
+    return None             # the march: bound by instruction issue, its voxel fetches depend on the rays
+
+
+def run_scale(args):
+    """The large-map configuration as a plain single session: 640x480 frames
+    along the figure-eight, 5 mm voxels, 2 cm truncation, 2^21 hash slots and a
+    2^20-block pool, photometric weight 0.1, marching cubes every 100 frames.
+    Pass 1 times every frame (gbf_process_frame, CUDA events on the stream) and
+    every mesh extraction; pass 2 runs the same frames as a batch of one with
+    CUDA events at the phase boundaries, for each phase's time and HBM rate."""
+    import torch
+    import libfusion_gb300 as L
+    from libfusion_gb300 import build as B
+    B.build()
+    K = intrinsics(L)
+    cfg = scale_config(L)
+    n = args.scale_frames
+    P = W * H
+    s_v = 12 if cfg.voxel_layout == L.VOXEL_REF else 8
+    sc = L.SynthScene(**SCALE_SCENE)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    bufs = [(torch.empty((H, W), dtype=torch.uint16, device="cuda"),
+             torch.empty((H, W, 3), dtype=torch.uint8, device="cuda")) for _ in range(2)]
+    max_tris = 1 << 24
+    vtx = torch.empty((max_tris, 3, 3), dtype=torch.float32, device="cuda")
+    truth = [sc.pose(k) for k in range(n)]
+
+    def render(k):
+        d, c = bufs[k & 1]
+        sc.render_into(K, k, d.data_ptr(), c.data_ptr(), stream=stream)
+        return d, c
+
+    # pass 1: the plain path, frame by frame
+    s = L.System(K, cfg)
+    s.set_pose(truth[0])
+    frame_ms, mesh_ms, tris, poses, failed = [], [], [], [], 0
+    for k in range(args.warmup):  # untimed warm-up on a throwaway session
+        w = L.System(K, cfg)
+        w.set_pose(truth[0])
+        w.process_images(*render(k), stream=stream)
+        w.close()
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        clocks.start()
+        for k in range(n):
+            d, c = render(k)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s.process_images(d, c, stream=stream)
+            b.record(stream)
+            frame_ms.append((a, b))
+            if (k + 1) % SCALE_MESH_EVERY == 0:
+                a2, b2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a2.record(stream)
+                tris.append(s.fetch_mesh_vertex_only(vtx, stream=stream))
+                b2.record(stream)
+                mesh_ms.append((a2, b2))
+            poses.append(s.get_camera_pose(stream=stream))
+            failed += 0 if s.stats(stream=stream).track.success else 1
+        torch.cuda.synchronize()
+        clocks.stop()
+    frame_ms = [a.elapsed_time(b) for a, b in frame_ms]
+    mesh_ms = [a.elapsed_time(b) for a, b in mesh_ms]
+    st = s.stats()
+    s.close()
+    total_ms = sum(frame_ms) + sum(mesh_ms)
+    poses = np.array(poses)
+    tr = np.array(truth)
+    err = np.linalg.norm(poses[:, :3, 3] - tr[:, :3, 3], axis=1)
+
+    # pass 2: the same frames as a batch of one, phase by phase
+    s2 = L.System(K, cfg)
+    s2.set_pose(truth[0])
+    b1 = L.FusionBatch(1)
+    b1.set(0, s2)
+    b1.set_groups(1)
+    b1.set_timing(True)
+    acc = {k: 0.0 for k in L.FusionBatch.PHASES}
+    work = {"pixel_iterations": 0, "integrated_blocks": 0, "allocated_blocks": 0, "visible_blocks": 0}
+    byt = {k: 0.0 for k in L.FusionBatch.PHASES}
+    prev = s2.stats()
+    for k in range(n):
+        d, c = render(k)
+        b1.set_inputs(0, d.data_ptr(), c.data_ptr())
+        b1.process([True], use_graph=False, stream=stream)
+        cur = s2.stats(stream=stream)
+        dd = {"pixel_iterations": cur.pixel_iterations - prev.pixel_iterations,
+              "integrated_blocks": cur.integrated_blocks - prev.integrated_blocks,
+              "allocated_blocks": cur.allocated_blocks, "visible_blocks": cur.visible_blocks}
+        for ph in byt:
+            x = phase_bytes(ph, P, cfg.num_levels, s_v, dd)
+            if x is not None:
+                byt[ph] += x
+        for key in work:
+            work[key] += dd[key]
+        prev = cur
+    ph = b1.phase_ms()
+    b1.close()
+    s2.close()
+    peak, peak_kind = measured_peaks()
+    phases = {}
+    for name in L.FusionBatch.PHASES:
+        ms = ph[name]
+        entry = {"ms_per_frame": ms}
+        if byt[name] > 0:
+            gbs = byt[name] / n / (ms / 1e3) / 1e9
+            entry.update({"algorithmic_bytes_per_frame": byt[name] / n, "gbs": gbs, "hbm_frac": gbs / peak})
+        else:
+            entry["bound"] = "instruction issue (voxel fetches depend on the rays; no algorithmic byte count)"
+        phases[name] = entry
+    mesh_bytes = [s_v * 512.0 * st.allocated_blocks + 36.0 * t for t in tris]
+    phases["mesh"] = {"ms_per_extraction": statistics.mean(mesh_ms) if mesh_ms else None,
+                      "extractions": len(mesh_ms), "triangles_last": tris[-1] if tris else 0,
+                      "gbs": (statistics.mean(mesh_bytes) / (statistics.mean(mesh_ms) / 1e3) / 1e9) if mesh_ms else None}
+    if mesh_ms:
+        phases["mesh"]["hbm_frac"] = phases["mesh"]["gbs"] / peak
+    lat = sorted(frame_ms)
+    q = lambda f: lat[min(len(lat) - 1, int(math.ceil(f * len(lat))) - 1)]
+    print(json.dumps({
+        "metric": METRIC, "workload": "scale", "value": n / (total_ms / 1e3), "unit": UNIT, "n_gpus": 1,
+        "steps": n, "warmup": args.warmup, "ms_per_step": total_ms / n, "higher_is_better": True,
+        "config": {"workload": f"plain single session at scale: {n} frames of 640x480 along a figure-eight "
+                               f"(0.5 m/s, 30 fps) in an 8x8x3 m room with 20 spheres and 12 boxes",
+                   "voxel_m": cfg.voxel_size, "truncation_m": cfg.truncation, "hash_slots": 1 << 21,
+                   "pool_blocks": 1 << 20, "voxel_layout": LAYOUTS[LAYOUT][1], "w_icp": cfg.w_icp,
+                   "w_rgb": cfg.w_rgb, "pyramid": "3 levels 10/5/3", "mesh_every": SCALE_MESH_EVERY},
+        "latency_ms": {"p50": q(0.5), "p99": q(0.99), "basis": "CUDA events around each frame's gbf_process_frame"},
+        "mesh_ms_total": sum(mesh_ms),
+        "phases": phases, "peak_gbs": peak, "peak_source": f"{peak_kind} hbm_gbs",
+        "work_per_frame": {k: v / n for k, v in work.items() if k in ("pixel_iterations", "integrated_blocks")},
+        "map": {"allocated_blocks": st.allocated_blocks, "status": st.status},
+        "tracking": {"failed_frames": failed, "ate_vs_ground_truth_mm": float(np.sqrt(np.mean(err ** 2)) * 1e3),
+                     "max_error_mm": float(err.max() * 1e3)},
+        "clocks": clocks.summary(),
+    }), flush=True)
+
+
 def main():
     global LAYOUT
     args = parse()
@@ -849,6 +1115,8 @@ def main():
         run_reference(args)
     elif args.workload == "mixed":
         run_mixed(args)
+    elif args.workload == "scale":
+        run_scale(args)
     else:
         run_ours(args)
 

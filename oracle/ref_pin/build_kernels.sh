@@ -1,6 +1,8 @@
 #!/bin/sh
-# Compile the reference's integration, z-range / raycast, ICP-row and
-# photometric-row kernels (src/voxel_hashing/depth_fusion.cu, ray_tracing.cu,
+# Compile the reference's integration, z-range / raycast, ICP-row,
+# photometric-row, image (derivative, back-projection, normals, shading) and
+# marching-cubes kernels (src/voxel_hashing/depth_fusion.cu, ray_tracing.cu,
+# scene_mesh.cu, src/tracking/cuda_imgproc.cu,
 # src/tracking/pose_estimator.cu, m_estimator.cu, with src/data_struct/
 # map_struct.cu for the map state, read where they lie under the reference
 # tree) into device modules for sm_103a, with the pin entry points of
@@ -18,7 +20,7 @@ OUT="$HERE/../_ref"
 mkdir -p "$OUT"
 FLAGS="-cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O3 -w --expt-relaxed-constexpr -I $REF/include -I $REF -I $HERE/stub_cv -I $HERE"
 pids=""
-for m in fusion raycast icp rgb; do
+for m in fusion raycast icp rgb imgproc mesh; do
     nvcc $FLAGS -fmad=false "$HERE/pin_$m.cu" -o "$OUT/pin_$m.cubin" & pids="$pids $!"
     nvcc $FLAGS "$HERE/pin_$m.cu" -o "$OUT/pin_${m}_fmad.cubin" & pids="$pids $!"
 done

@@ -24,12 +24,12 @@ __device__ inline fusion::Matrix3x4f m34(const float *p) {
 // (src/data_struct/map_struct.cu:10), uploaded by MapStruct's constructor.
 extern "C" __global__ void pin_set_state(int num_buckets, int num_entries, int num_blocks, float voxel_size,
                                          float zmin_raycast, float zmax_raycast, float zmin_update,
-                                         float zmax_update, int max_rendering_blocks) {
+                                         float zmax_update, int max_rendering_blocks, int max_mesh_triangles) {
     fusion::MapState s;
     s.num_total_buckets_ = num_buckets;
     s.num_total_hash_entries_ = num_entries;
     s.num_total_voxel_blocks_ = num_blocks;
-    s.num_max_mesh_triangles_ = 0;
+    s.num_max_mesh_triangles_ = max_mesh_triangles;
     s.num_max_rendering_blocks_ = max_rendering_blocks;
     s.zmin_raycast = zmin_raycast;
     s.zmax_raycast = zmax_raycast;

@@ -15,11 +15,23 @@ typedef unsigned char uchar;
 #define CV_8UC1 0
 #define CV_32SC1 4
 #define CV_32FC1 5
+#define CV_32FC4 29
+#define CV_8UC4 24
 
 namespace cv {
 
 struct Scalar {
     Scalar(double v0, double v1 = 0, double v2 = 0, double v3 = 0);
+};
+
+struct Size {
+    int width, height;
+    Size(int w, int h);
+};
+
+struct KeyPoint {
+    float pt[2], size, angle, response;
+    int octave, class_id;
 };
 
 class Mat {
@@ -61,6 +73,9 @@ public:
     uchar *data;
     bool empty() const;
     void create(int rows, int cols, int type);
+    void create(Size size, int type);
+    Size size() const;
+    int type() const;
     GpuMat &setTo(Scalar s);
     void download(Mat &m) const;
     template <typename T> T *ptr(int y = 0);
@@ -70,6 +85,9 @@ public:
 };
 
 void reduce(const GpuMat &src, GpuMat &dst, int dim, int reduce_op, int dtype = -1);
+void resize(const GpuMat &src, GpuMat &dst, Size dsize, double fx = 0, double fy = 0, int interpolation = 1);
+void pyrDown(const GpuMat &src, GpuMat &dst);
+void bilateralFilter(const GpuMat &src, GpuMat &dst, int kernel_size, float sigma_color, float sigma_spatial);
 
 }  // namespace cuda
 }  // namespace cv

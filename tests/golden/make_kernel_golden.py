@@ -33,6 +33,7 @@ import pin_cases as P  # noqa: E402
 REF = ROOT / "oracle" / "_ref"
 REF_BLOCKS = 100000  # num_max_rendering_blocks_, the MapStruct default (map_struct.cu:27)
 # RenderingBlock (include/data_struct/map_struct.h:62-67): Vector2s upper_left, lower_right; Vector2f zrange
+SENTINEL = 12345.0  # what a pixel the image kernels do not write keeps
 RENDERING_BLOCK = np.dtype([("upper_left", "<i2", 2), ("lower_right", "<i2", 2), ("zrange", "<f4", 2)])
 
 
@@ -46,18 +47,19 @@ class Reference:
     def __init__(self, suffix: str = ""):
         import cudrv
         self.cu = cudrv
-        self.m = {k: cudrv.Module(REF / f"pin_{k}{suffix}.cubin") for k in ("fusion", "raycast", "icp", "rgb")}
+        self.m = {k: cudrv.Module(REF / f"pin_{k}{suffix}.cubin")
+                  for k in ("fusion", "raycast", "icp", "rgb", "imgproc", "mesh")}
         import torch
         sz = torch.zeros(4, dtype=torch.int32, device="cuda")
         self.m["fusion"].function("pin_sizes").launch((1,), (1,), [ptr(sz)])
         # Voxel, HashEntry, RenderingBlock, MapState as the reference's headers lay them out
         assert sz.cpu().tolist() == [12, 20, 16, 40], sz.cpu().tolist()
 
-    def set_state(self, mod: str, n_buckets: int, n_entries: int, n_blocks: int):
+    def set_state(self, mod: str, n_buckets: int, n_entries: int, n_blocks: int, max_triangles: int = 0):
         f = C.c_float
         self.m[mod].function("pin_set_state").launch(
             (1,), (1,), [C.c_int(n_buckets), C.c_int(n_entries), C.c_int(n_blocks), f(P.VOXEL), f(P.ZMIN), f(P.ZMAX),
-                         f(P.ZMIN), f(P.ZMAX), C.c_int(REF_BLOCKS)])
+                         f(P.ZMIN), f(P.ZMAX), C.c_int(REF_BLOCKS), C.c_int(max_triangles)])
 
     def state_values(self, mod: str):
         import torch
@@ -184,6 +186,89 @@ class Reference:
         return out_icp.cpu().numpy(), out_rgb.cpu().numpy()
 
 
+    # ------------------------------------------------------------- image kernels
+    def images(self, depth, intensity, level):
+        """backProjectDepthK, computeNMapK of its output, computeDerivativeK
+        of the intensity; pixels a kernel does not write keep SENTINEL."""
+        import torch
+        cu, vp = self.cu, C.c_void_p
+        h, w = depth.shape
+        fx, fy, cx, cy = (np.float32(v) for v in (P.FX, P.FY, P.CX, P.CY))
+        for _ in range(level):  # IntrinsicMatrix::pyr_down (intrinsic_matrix.h:33-37)
+            fx, fy, cx, cy = (np.float32(0.5) * v for v in (fx, fy, cx, cy))
+        K = cu.struct_bytes((C.c_int, w), (C.c_int, h), (C.c_float, fx), (C.c_float, fy), (C.c_float, cx),
+                            (C.c_float, cy), (C.c_float, np.float32(1.0) / fx), (C.c_float, np.float32(1.0) / fy))
+        dd = torch.from_numpy(np.ascontiguousarray(depth, np.float32)).cuda()
+        di = torch.from_numpy(np.ascontiguousarray(intensity, np.float32)).cuda()
+        vm = torch.full((h, w, 4), SENTINEL, dtype=torch.float32, device="cuda")
+        nm = torch.full((h, w, 4), SENTINEL, dtype=torch.float32, device="cuda")
+        dx = torch.full((h, w), SENTINEL, dtype=torch.float32, device="cuda")
+        dy = torch.full((h, w), SENTINEL, dtype=torch.float32, device="cuda")
+        sz = lambda t, step: cu.struct_bytes((vp, t.data_ptr()), (C.c_size_t, step), (C.c_int, w), (C.c_int, h))
+        st = lambda t, step: cu.struct_bytes((vp, t.data_ptr()), (C.c_size_t, step))
+        grid, blk = ((w + 7) // 8, (h + 7) // 8), (8, 8)
+        mod = self.m["imgproc"]
+        mod.function("backProjectDepthK").launch(grid, blk, [sz(dd, w * 4), st(vm, w * 16), K])
+        mod.function("computeNMapK").launch(grid, blk, [sz(vm, w * 16), st(nm, w * 16)])
+        mod.function("computeDerivativeK").launch(grid, blk, [sz(di, w * 4), st(dx, w * 4), st(dy, w * 4)])
+        return {"vmap": P.canonical_nan(vm.cpu().numpy()), "nmap": P.canonical_nan(nm.cpu().numpy()),
+                "dx": dx.cpu().numpy(), "dy": dy.cpu().numpy()}
+
+    def shading(self, vmap, nmap, rgb):
+        """renderSceneK and renderSceneTexturedK, light at (5, 5, 5) (cuda_imgproc.cu:69-108)."""
+        import torch
+        cu, vp = self.cu, C.c_void_p
+        h, w = vmap.shape[:2]
+        dv = torch.from_numpy(np.ascontiguousarray(vmap, np.float32)).cuda()
+        dn = torch.from_numpy(np.ascontiguousarray(nmap, np.float32)).cuda()
+        dc = torch.from_numpy(np.ascontiguousarray(rgb, np.uint8)).cuda()
+        light = cu.struct_bytes((C.c_float, 5.0), (C.c_float, 5.0), (C.c_float, 5.0))
+        st = lambda t, step: cu.struct_bytes((vp, t.data_ptr()), (C.c_size_t, step))
+        out = []
+        for textured in (False, True):
+            dst = torch.zeros((h, w, 4), dtype=torch.uint8, device="cuda")
+            dsz = cu.struct_bytes((vp, dst.data_ptr()), (C.c_size_t, w * 4), (C.c_int, w), (C.c_int, h))
+            grid, blk = ((w + 7) // 8, (h + 7) // 8), (8, 8)
+            if textured:
+                self.m["imgproc"].function("renderSceneTexturedK").launch(
+                    grid, blk, [st(dv, w * 16), st(dn, w * 16), st(dc, w * 3), light, dsz])
+            else:
+                self.m["imgproc"].function("renderSceneK").launch(grid, blk, [st(dv, w * 16), st(dn, w * 16), light, dsz])
+            out.append(dst.cpu().numpy())
+        return out
+
+    # ------------------------------------------------------------- marching cubes
+    def mesh(self, dump, max_triangles=1 << 20):
+        """create_mesh_with_normal and create_mesh_with_colour over a map in
+        the reference's chained-table layout: (vertices, normals), (vertices,
+        colours), each in canonical order."""
+        import torch
+        nb, ne, nbk = dump["size"]
+        self.set_state("mesh", nbk, ne, nb, max_triangles)
+        vox = torch.from_numpy(dump["voxels"].view(np.uint8).copy()).cuda()
+        table = torch.from_numpy(dump["table"].view(np.uint8).copy()).cuda()
+        out = []
+        for select, make, attr in (("pin_mesh_select", "pin_mesh_normals", (np.float32, 3)),
+                                   ("pin_mesh_colour_select", "pin_mesh_colour", (np.uint8, 3))):
+            blocks = torch.zeros(ne * 20, dtype=torch.uint8, device="cuda")
+            nblk = torch.zeros(1, dtype=torch.int32, device="cuda")
+            ntri = torch.zeros(1, dtype=torch.int32, device="cuda")
+            tri = torch.zeros((max_triangles, 3, 3), dtype=torch.float32, device="cuda")
+            att = torch.zeros((max_triangles, 3, 3), dtype=torch.float32 if attr[0] == np.float32 else torch.uint8,
+                              device="cuda")
+            self.m["mesh"].function(select).launch(((ne + 1023) // 1024,), (1024,),
+                                                   [ptr(vox), ptr(table), ptr(blocks), ptr(nblk)])
+            bc = int(nblk.cpu().item())
+            self.m["mesh"].function(make).launch(((bc + 15) // 16, 16), (8, 8),
+                                                 [ptr(vox), ptr(table), ptr(blocks), ptr(nblk), ptr(ntri), ptr(tri),
+                                                  ptr(att)])
+            n = int(ntri.cpu().item())
+            assert n < max_triangles
+            v, a = P.sort_triangles(tri[:n].cpu().numpy(), att[:n].cpu().numpy())
+            out.append((P.canonical_nan(v), P.canonical_nan(a) if attr[0] == np.float32 else a))
+        return out
+
+
 def ref_state(coords, vox):
     return P.canonical_state(coords, vox["sdf"], vox["weight"], vox["rgb"])
 
@@ -233,6 +318,13 @@ def run_all(ref: Reference, L, O, dep, rgb, poses, oc):
     for k, T in enumerate(P.raycast_poses(poses)):
         z, v, nr = ref.raycast(dump, oc["visible_b"], T)
         out[f"zrange_{k}"], out[f"vmap_{k}"], out[f"render_blocks_{k}"] = z, P.canonical_nan(v), nr
+    (out["mesh_normal_v"], out["mesh_normal_n"]), (out["mesh_colour_v"], out["mesh_colour_c"]) = ref.mesh(dump)
+    # image kernels and shading on frame B's images
+    im = P.oracle_images(L, O, dep, rgb)
+    for level in P.LEVELS:
+        for k, v in ref.images(im[level]["depth"], im[level]["intensity"], level).items():
+            out[f"img_{k}_{level}"] = v
+    out["shade"], out["shade_textured"] = ref.shading(im[0]["vmap"], im[0]["nmap"], rgb[1])
     # rows
     fr = P.oracle_frames(L, O, dep, rgb)
     T = P.relative(poses[0], poses[1])
@@ -268,6 +360,26 @@ def compare_with_oracle(L, O, dep, rgb, poses, got) -> dict:
             icp, pho = P.oracle_rows(O, fr[0], fr[1], level, T, sd)
             rep[f"icp_{level}"] = bool(np.array_equal(icp.view(np.int32), got[f"icp_{level}"].view(np.int32)))
             rep[f"rgb_{level}_{sd:g}"] = bool(np.array_equal(pho.view(np.int32), got[f"rgb_{level}_{sd:g}"].view(np.int32)))
+    om, _ = P.oracle_raycasts(L, O, dep, rgb, poses, ())
+    (vn, nn), (vc, cc) = P.oracle_meshes(om)
+    rep["mesh"] = {"triangles": int(len(got["mesh_normal_v"])), "oracle_triangles": int(len(vn)),
+                   "normal_mesh": bool(len(vn) == len(got["mesh_normal_v"]) and np.array_equal(
+                       vn.view(np.int32), got["mesh_normal_v"].view(np.int32)) and np.array_equal(
+                       nn.view(np.int32), got["mesh_normal_n"].view(np.int32))),
+                   "colour_mesh": bool(len(vc) == len(got["mesh_colour_v"]) and np.array_equal(
+                       vc.view(np.int32), got["mesh_colour_v"].view(np.int32)) and np.array_equal(
+                       cc, got["mesh_colour_c"]))}
+    im = P.oracle_images(L, O, dep, rgb)
+    for level in P.LEVELS:
+        for k in ("vmap", "nmap", "dx", "dy"):
+            a, b = P.interior(im[level][k]), P.interior(got[f"img_{k}_{level}"])
+            if k == "vmap":
+                a, b = im[level][k], got[f"img_{k}_{level}"]
+            rep[f"img_{k}_{level}"] = bool(np.array_equal(a.view(np.int32), b.view(np.int32)))
+    s0, s1 = P.oracle_shading(O, dep, rgb, im)
+    for name, a, b in (("shade", s0, got["shade"]), ("shade_textured", s1, got["shade_textured"])):
+        d = np.abs(a.astype(int) - b.astype(int))
+        rep[name] = {"pixels_differing": int(np.sum(d.max(axis=-1) > 0)), "max_diff": int(d.max())}
     return rep
 
 
@@ -286,6 +398,10 @@ def contraction_report(a: dict, b: dict) -> dict:
                             "max_abs_z_diff_m": float(np.abs(va[..., 2][both] - vb[..., 2][both]).max())
                             if both.any() else 0.0,
                             "vertices_differing": int(np.sum(np.any(va[both] != vb[both], axis=-1)))}
+    rep["mesh_triangles"] = [int(len(a["mesh_normal_v"])), int(len(b["mesh_normal_v"]))]
+    for k in ("img_vmap_0", "img_nmap_0", "img_dx_0", "img_dy_0", "shade", "shade_textured"):
+        rep[k] = {"values_differing": int(np.sum(a[k].view(np.uint8 if a[k].dtype == np.uint8 else np.int32) !=
+                                                 b[k].view(np.uint8 if b[k].dtype == np.uint8 else np.int32)))}
     for k in a:
         if k.startswith(("icp_", "rgb_")):
             x, y = a[k], b[k]
@@ -348,6 +464,19 @@ def main() -> None:
             fx[f"{k}_digest"] = np.array(P.digest(got[k]))
             fx[f"{k}_sample"] = got[k][s]
             fx[f"{k}_found"] = np.packbits(got[k][:, 28] != 0)
+    for k in ("normal", "colour"):
+        v, att = got[f"mesh_{k}_v"], got[f"mesh_{k}_{k[0]}"]
+        s = P.sample_triangles(len(v))
+        fx[f"mesh_{k}_digest"] = np.array(P.digest(v, att))
+        fx[f"mesh_{k}_count"] = np.array(len(v))
+        fx[f"mesh_{k}_sample_v"], fx[f"mesh_{k}_sample_a"] = v[s], att[s]
+    for level in P.LEVELS:
+        fx[f"img_vmap_{level}_digest"] = np.array(P.digest(got[f"img_vmap_{level}"]))
+        fx[f"img_nmap_{level}_digest"] = np.array(P.digest(P.interior(got[f"img_nmap_{level}"])))
+        fx[f"img_nmap_{level}_border_unwritten"] = np.array(bool(
+            np.all(got[f"img_nmap_{level}"][-1] == SENTINEL) and np.all(got[f"img_nmap_{level}"][:, -1] == SENTINEL)))
+        fx[f"img_dx_{level}"], fx[f"img_dy_{level}"] = got[f"img_dx_{level}"], got[f"img_dy_{level}"]
+    fx["shade"], fx["shade_textured"] = got["shade"], got["shade_textured"]
     fx["report"] = np.array(json.dumps(report))
     out_path.parent.mkdir(parents=True, exist_ok=True)
     np.savez_compressed(out_path, **fx)

@@ -200,3 +200,55 @@ def oracle_rows(O, ref, cur, level, T, stddev):
 def sample_pixels(n_pixels: int, level: int) -> np.ndarray:
     rng = np.random.default_rng(1000 + level)
     return np.sort(rng.choice(n_pixels, size=min(N_SAMPLE, n_pixels), replace=False))
+
+
+# ---------------------------------------------------------------- image kernels
+
+def oracle_images(L, O, depth_u16, rgb):
+    """Frame B's images at the pinned levels: the kernels' inputs (metric
+    depth, intensity) and the oracle's outputs (vertex and normal maps,
+    gradients)."""
+    f = oracle_frames(L, O, depth_u16, rgb)[1]
+    return {level: {"depth": f.get(5, level), "intensity": f.get(2, level), "vmap": canonical_nan(f.get(0, level)),
+                    "nmap": canonical_nan(f.get(1, level)), "dx": f.get(3, level), "dy": f.get(4, level)}
+            for level in LEVELS}
+
+
+def interior(a: np.ndarray) -> np.ndarray:
+    """All but the last row and column: computeDerivativeK and computeNMapK
+    write nothing there (cuda_imgproc.cu:224, :280)."""
+    return a[:-1, :-1]
+
+
+def oracle_shading(O, depth_u16, rgb, images):
+    """renderScene and renderSceneTextured of frame B's level-0 maps."""
+    im = images[0]
+    return O.render_scene(im["vmap"], im["nmap"]), O.render_scene(im["vmap"], im["nmap"], rgb[1])
+
+
+# ---------------------------------------------------------------- marching cubes
+
+def sort_triangles(v, *attrs):
+    """Canonical order of a triangle soup: by the 9 vertex coordinates, ties by
+    the attributes (NaN normals of degenerate triangles last)."""
+    cols = [v.reshape(len(v), 9)[:, i] for i in range(9)]
+    for a in attrs:
+        flat = a.reshape(len(a), -1).astype(np.float64)
+        cols += [np.nan_to_num(flat[:, i], nan=1e30) for i in range(flat.shape[1])]
+    order = np.lexsort(cols[::-1])
+    return (v[order],) + tuple(a[order] for a in attrs)
+
+
+def oracle_meshes(om):
+    """Marching cubes of a map: (vertices, normals) and (vertices, colours),
+    each in canonical order, NaN canonical."""
+    v1, n1 = om.mesh(1, 1 << 20)
+    v2, c2 = om.mesh(2, 1 << 20)
+    a = sort_triangles(v1, n1)
+    b = sort_triangles(v2, c2)
+    return (canonical_nan(a[0]), canonical_nan(a[1])), (canonical_nan(b[0]), b[1])
+
+
+def sample_triangles(n: int) -> np.ndarray:
+    rng = np.random.default_rng(77)
+    return np.sort(rng.choice(n, size=min(1024, n), replace=False))

@@ -6,11 +6,14 @@ tests/golden/ref_kernels.npz holds what the reference's integration
 src/voxel_hashing/depth_fusion.cu:288-428), z-range tiles
 (RenderingBlockDelegate, ray_tracing.cu:17-277), raycast march
 (MapRenderingDelegate::operator(), ray_tracing.cu:346-425), ICP row
-(ICPReduction::getRow, src/tracking/pose_estimator.cu:166-222) and
-photometric row (RgbReduction2::compute_jacobian, m_estimator.cu:313-391)
-computed on a GB300 from the reference sources, built with every float
-operation rounded as written (tests/golden/make_kernel_golden.py; cases in
-tests/golden/pin_cases.py).
+(ICPReduction::getRow, src/tracking/pose_estimator.cu:166-222), photometric
+row (RgbReduction2::compute_jacobian, m_estimator.cu:313-391), image kernels
+(computeDerivativeK, backProjectDepthK, computeNMapK, renderSceneK,
+renderSceneTexturedK: src/tracking/cuda_imgproc.cu:17-305) and marching cubes
+(BuildVertexArray, BuildVertexAndColourArray: src/voxel_hashing/
+scene_mesh.cu:14-643) computed on a GB300 from the reference sources, built
+with every float operation rounded as written
+(tests/golden/make_kernel_golden.py; cases in tests/golden/pin_cases.py).
 
 CPU tests: the oracle recomputes every case from the stored frames.  Integer
 and float results are compared bit for bit, except the normal-weighted update,
@@ -19,7 +22,8 @@ the oracle (a few ulp apart): there the sdf codes may differ by one
 truncation step and the colours by one level, on a small share of the voxels.
 
 GPU tests: the CUDA kernels on the same inputs match the reference's outputs
-bit for bit, the normal-weighted update included (both use CUDA's sinf).
+bit for bit, the normal-weighted update included (both use CUDA's sinf), and
+so do the marching cubes and the shading (CUDA's powf on both sides).
 """
 from pathlib import Path
 import sys
@@ -173,3 +177,99 @@ def test_gpu_raycast_matches_reference_kernels(gbf, fx):
         m.raycast(vm, T)
         v = P.canonical_nan(vm.cpu().numpy())
         assert np.array_equal(v.view(np.int32), fx[f"vmap_{k}"].view(np.int32)), k
+
+
+# ------------------------------------------------------------------ image kernels, shading, marching cubes
+
+
+@pytest.fixture(scope="module")
+def images(fx, lib, oracle_mod):
+    d, c, _ = frames(fx)
+    return P.oracle_images(lib, oracle_mod, d, c)
+
+
+@pytest.mark.parametrize("level", P.LEVELS)
+def test_image_kernels_bit_exact(fx, images, level):
+    """backProjectDepthK, computeNMapK and computeDerivativeK
+    (src/tracking/cuda_imgproc.cu:217-305) on the oracle's level-`level`
+    depth and intensity.  The reference leaves the last row and column of
+    the normal and gradient maps unwritten; there the oracle writes NaN
+    normals and zero gradients."""
+    im = images[level]
+    assert P.digest(im["vmap"]) == str(fx[f"img_vmap_{level}_digest"])
+    assert P.digest(P.interior(im["nmap"])) == str(fx[f"img_nmap_{level}_digest"])
+    assert bool(fx[f"img_nmap_{level}_border_unwritten"])
+    for k in ("dx", "dy"):
+        ref = fx[f"img_{k}_{level}"]
+        assert np.array_equal(P.interior(im[k]).view(np.int32), P.interior(ref).view(np.int32)), k
+        assert np.all(ref[-1] == 12345.0) and np.all(ref[:, -1] == 12345.0)  # unwritten by the reference
+
+
+def test_shading_matches_reference(fx, images):
+    """renderSceneK / renderSceneTexturedK (cuda_imgproc.cu:17-108): the
+    specular term takes CUDA's powf in the reference and libm's in the
+    oracle, so a channel may differ by one level on a few pixels; on this
+    frame none does."""
+    d, c, _ = frames(fx)
+    import oracle as O
+    plain, textured = P.oracle_shading(O, d, c, images)
+    for got, key in ((plain, "shade"), (textured, "shade_textured")):
+        diff = np.abs(got.astype(int) - fx[key].astype(int))
+        assert diff.max() <= 1 and np.mean(diff.max(axis=-1) > 0) < 2e-3, key
+
+
+@pytest.fixture(scope="module")
+def meshes(fx, lib, oracle_mod):
+    d, c, poses = frames(fx)
+    om, _ = P.oracle_raycasts(lib, oracle_mod, d, c, poses, ())
+    return P.oracle_meshes(om)
+
+
+@pytest.mark.parametrize("kind", ["normal", "colour"])
+def test_marching_cubes_bit_exact(fx, meshes, kind):
+    """create_mesh_with_normal / create_mesh_with_colour (src/voxel_hashing/
+    scene_mesh.cu:14-643) of the map after frames A and B, as triangle sets
+    (the reference appends triangles in atomic order)."""
+    v, a = meshes[0] if kind == "normal" else meshes[1]
+    assert len(v) == int(fx[f"mesh_{kind}_count"]) and len(v) > 50000
+    s = P.sample_triangles(len(v))
+    assert np.array_equal(v[s].view(np.int32), fx[f"mesh_{kind}_sample_v"].view(np.int32))
+    assert np.array_equal(a[s].view(np.int32 if kind == "normal" else np.uint8), fx[f"mesh_{kind}_sample_a"].view(
+        np.int32 if kind == "normal" else np.uint8))
+    assert P.digest(v, a) == str(fx[f"mesh_{kind}_digest"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["normal", "colour"])
+def test_gpu_marching_cubes_matches_reference_kernels(gbf, fx, kind):
+    import torch
+    L = gbf
+    m = _gpu_map(L, fx)
+    cap = int(fx[f"mesh_{kind}_count"]) + 64
+    vtx = torch.zeros((cap, 3, 3), dtype=torch.float32, device="cuda")
+    if kind == "normal":
+        attr = torch.zeros((cap, 3, 3), dtype=torch.float32, device="cuda")
+        n = m.fetch_mesh_with_normal(vtx, attr)
+    else:
+        attr = torch.zeros((cap, 3, 3), dtype=torch.uint8, device="cuda")
+        n = m.fetch_mesh_with_colour(vtx, attr)
+    assert n == int(fx[f"mesh_{kind}_count"])
+    v, a = P.sort_triangles(vtx[:n].cpu().numpy(), attr[:n].cpu().numpy())
+    v = P.canonical_nan(v)
+    a = P.canonical_nan(a) if kind == "normal" else a
+    assert P.digest(v, a) == str(fx[f"mesh_{kind}_digest"])
+
+
+@pytest.mark.gpu
+def test_gpu_shading_matches_reference_kernels(gbf, fx, images):
+    L = gbf
+    im = images[0]
+    _, c, _ = frames(fx)
+    plain = L.render_scene(H_cuda(im["vmap"]), H_cuda(im["nmap"])).cpu().numpy()
+    textured = L.render_scene(H_cuda(im["vmap"]), H_cuda(im["nmap"]), H_cuda(c[1])).cpu().numpy()
+    assert np.array_equal(plain, fx["shade"]) and np.array_equal(textured, fx["shade_textured"])
+
+
+def H_cuda(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
