@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="fixed launch shape instead of the batch's tuner")
     ap.add_argument("--tune-ticks", type=int, default=6, help="timed ticks per tuner candidate")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--serve-ticks", type=int, default=120, help="ticks of the churn (arrival / eviction) run")
+    ap.add_argument("--serve-seconds", type=float, default=40.0,
+                    help="wall-clock seconds of the continuous-batching serving run (0: skip)")
     ap.add_argument("--layout", default="snorm", choices=sorted(LAYOUTS), help="voxel storage of every session")
     ap.add_argument("--precision-frames", type=int, default=PREC_FRAMES,
                     help="frames of the precision check against the FP64 oracle (0: skip)")
@@ -478,60 +479,103 @@ def host_frames(L, K, n, seed=0):
     return out
 
 
-def serve_churn(L, K, args, batch, sessions, frames, first, n_ticks, budget, stream):
-    """Config-5 style serving after the steady-state measurement: camera frames
-    at 30 fps, sessions arriving as a Poisson process of 4/s while the batch
-    holds its 64 concurrent sessions -- each arrival takes the slot of the
-    longest-running session, which closes: the slot's session is reset
-    (gbf_session_reset, map and tracking state cleared, device memory kept) and
-    starts the newcomer's sequence, so admission needs no allocation and the
-    captured tick stays valid.  Per tick: admission, staging, the tick, its
-    results on the host; latency = host wall clock for that (each frame arrives
-    at its tick's start).  The newcomers' synthetic frames are rendered before
-    the timed ticks (the harness's work, not the server's)."""
+# the served configuration: Poisson arrivals at 4/s, up to 64 concurrent 640x480
+# sessions at 30 fps for 300-3000 frames, voxel sizes of 5-10 mm, admission by
+# device memory under a 150 GB budget
+SERVE_VOXELS_MM = (5, 6, 7, 8, 9, 10)
+SERVE_SCENES = 16        # distinct synthetic rooms the cameras film
+SERVE_SWEEP = 120        # frames of a room's pre-rendered sweep, played back and forth
+
+
+def serve_pool(v_mm: int) -> int:
+    """Block pool of a session: a 4x4x3 m room's surfaces at v mm, with room to spare."""
+    return 1 << 20 if v_mm < 6 else (1 << 19 if v_mm < 8 else 1 << 18)
+
+
+def serve_config(L, v_mm: int):
+    v = v_mm / 1000.0
+    pool = serve_pool(v_mm)
+    return L.default_config(voxel_size=v, truncation=min(max(3.0 * v, 0.02), 0.03), zmin_update=0.3,
+                            zmax_update=4.0, zmin_raycast=0.3, zmax_raycast=4.0, num_buckets=2 * pool,
+                            num_blocks=pool, voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3,
+                            max_iterations=[10, 5, 3, 3, 3], max_probe=256)
+
+
+def serve_run(L, K, seconds: float, groups: int, stream, rate: float = 4.0, slots: int = 64,
+              budget: int = 150 * (1 << 30), seed: int = 12345):
+    """Config-5 serving, continuous batching (libfusion_gb300/serving.py), in
+    real time for `seconds`: requests arrive as a Poisson process of `rate`/s,
+    each a camera streaming 640x480 frames at 30 fps for 300-3000 frames with
+    a voxel size of 5-10 mm; a request is admitted when one of `slots` batch
+    slots is free and its session arena fits the device budget
+    (gbf_session_bytes), its camera then streams, every tick fuses one frame of
+    each session whose next frame has arrived, and a session is evicted after
+    its last frame (its arena cached for reuse).  The cameras film
+    SERVE_SCENES synthetic rooms whose frames are rendered beforehand (a sweep
+    of SERVE_SWEEP frames played forwards and backwards, a continuous camera
+    motion), so no rendering competes with the server for the GPU."""
     import torch
-    if n_ticks <= 0:
-        return None
-    rng = np.random.default_rng(12345)
-    S = len(sessions)
-    arrive = [k for k in range(n_ticks) if rng.random() < 4.0 / 30.0]  # Poisson rate 4/s per 1/30 s tick
-    new_frames = {k: render_frames(L, K, [50000 + j], n_ticks - k) for j, k in enumerate(arrive)}
-    used = sum(L.session_bytes(session_config(L, i), K) for i in range(S))
-    assert used <= budget
-    started = [0] * S       # tick at which each slot's session started
-    cursor = [first] * S    # next frame index of each slot's sequence
-    seq = [frames[i] for i in range(S)]
-    active = [True] * S
-    lat = []
-    for k in range(-1, n_ticks):  # tick -1: untimed, re-captures the graphs after the timing pass
-        if k == 0:
-            torch.cuda.synchronize()
-            t_all = time.perf_counter()
-        t0 = time.perf_counter()
-        if k in new_frames:
-            slot = int(np.argmin(started))      # the longest-running session closes
-            fr_new, poses_new = new_frames[k]
-            sessions[slot].reset(stream)
-            sessions[slot].set_pose(poses_new[0], stream)
-            seq[slot], cursor[slot], started[slot] = fr_new[0], 0, k
-        for i in range(S):
-            d, c = seq[i]
-            j = min(cursor[i], d.shape[0] - 1)
-            batch.set_inputs(i, d[j].data_ptr(), c[j].data_ptr())
-            cursor[i] += 1
-        batch.process(active, use_graph=not args.no_graph, stream=stream)
-        batch.results(back=0)                   # the tick's poses on the host
-        if k >= 0:
-            lat.append((time.perf_counter() - t0) * 1e3)
-    wall = time.perf_counter() - t_all
-    batch.flush()
-    lat.sort()
-    q = lambda f: lat[min(len(lat) - 1, int(math.ceil(f * len(lat))) - 1)]
-    return {"ticks": n_ticks, "arrivals": len(arrive), "value": S * n_ticks / wall, "unit": UNIT,
-            "latency_ms": {"p50": q(0.5), "p95": q(0.95), "p99": q(0.99), "max": lat[-1]},
-            "model": "Poisson arrivals 4/s at 30 fps ticks, 64 concurrent sessions under the 150 GB budget: an "
-                     "arrival takes the longest-running session's slot (session reset, memory kept); latency = "
-                     "host wall clock per tick including admission, staging and result read-back"}
+    from libfusion_gb300.serving import ArenaCache, Request, Server
+    rng = np.random.default_rng(seed)
+    sweep = []
+    for i in range(SERVE_SCENES):
+        sc = L.SynthScene(seed=70000 + i)
+        d = torch.empty((SERVE_SWEEP, H, W), dtype=torch.uint16, device="cuda")
+        c = torch.empty((SERVE_SWEEP, H, W, 3), dtype=torch.uint8, device="cuda")
+        for k in range(SERVE_SWEEP):
+            sc.render_into(K, k, d[k].data_ptr(), c[k].data_ptr())
+        sweep.append((d, c, sc.pose(0)))
+        sc.close()
+    torch.cuda.synchronize()
+
+    def source(scene):
+        d, c, _ = sweep[scene]
+        period = 2 * SERVE_SWEEP - 2
+
+        def frame(k):
+            j = k % period
+            j = j if j < SERVE_SWEEP else period - j
+            return d[j].data_ptr(), c[j].data_ptr()
+        return frame
+
+    cfgs = {v: serve_config(L, v) for v in SERVE_VOXELS_MM}
+    nbytes = {v: L.session_bytes(cfgs[v], K) for v in SERVE_VOXELS_MM}
+    reqs, t, sid = [], 0.0, 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        v = int(rng.choice(SERVE_VOXELS_MM))
+        scene = sid % SERVE_SCENES
+        reqs.append(Request(sid=sid, arrival=t, frames=int(rng.integers(300, 3001)), key=(v,), nbytes=nbytes[v],
+                            pose0=sweep[scene][2], source=source(scene)))
+        sid += 1
+    batch = L.FusionBatch(slots)
+    batch.reserve(K, cfgs[min(SERVE_VOXELS_MM)], slots)  # the largest session: the tick's shape never changes
+    batch.set_groups(groups)
+    cache = ArenaCache(budget, make=lambda key: L.System(K, cfgs[key[0]]), destroy=lambda s: s.close(),
+                       reset=lambda s: s.reset(stream))
+    srv = Server(batch, slots, cache, set_pose=lambda s, T: s.set_pose(T, stream), stream=stream)
+    for r in reqs:
+        srv.submit(r)
+    srv.run(seconds)
+    rep = srv.report()
+    for slot, x in enumerate(srv.live):
+        if x is not None:
+            batch.set(slot, None)
+            x.session.close()
+    batch.close()
+    cache.close()
+    del sweep
+    torch.cuda.synchronize()
+    rep["model"] = (f"Poisson arrivals {rate}/s for {seconds:.0f} s of wall time, up to {slots} concurrent 640x480 "
+                    f"sessions, cameras at 30 fps for 300-3000 frames, voxel {SERVE_VOXELS_MM[0]}-"
+                    f"{SERVE_VOXELS_MM[-1]} mm (block pools of 2^18-2^20), admitted when a slot is free and the "
+                    f"session's arena fits the {budget / (1 << 30):.0f} GiB budget, evicted after the last frame; "
+                    "latency from a frame's capture (admission + index / 30 fps) to its pose on the host")
+    rep["session_bytes_by_voxel_mm"] = {str(v): nbytes[v] for v in SERVE_VOXELS_MM}
+    rep["graph_shape_reserved"] = f"{slots} slots of the largest session (pool {serve_pool(min(SERVE_VOXELS_MM))})"
+    return rep
 
 
 # ----------------------------------------------------------------------------- arms
@@ -586,8 +630,7 @@ def run_ours(args):
     S = args.sessions
     steps, warm = args.steps, args.warmup
     n_phase = min(steps, 8)
-    n_serve = args.serve_ticks
-    nfr = warm + steps + n_phase + n_serve
+    nfr = warm + steps + n_phase
     # the tuner's search: 10 candidates, each timed for --tune-ticks ticks after
     # one untimed tick, plus the two ticks in flight at every switch
     n_tune = 0 if args.no_autotune else 10 * (args.tune_ticks + 3) + 10
@@ -668,7 +711,6 @@ def run_ours(args):
     bad = [i for i, st in enumerate(status) if st.status & ~L.FLAG_TRACK_FAILED]
     failed = sum(1 for st in status if st.status & L.FLAG_TRACK_FAILED)
 
-    serving = serve_churn(L, K, args, batch, sessions, frames, warm + steps + n_phase, n_serve, budget, stream)
 
     # roofline of the dominant kernel phase: algorithmic bytes of the work the
     # phase's launches did, over their CUDA-event time (the mean launch)
@@ -800,6 +842,11 @@ def run_ours(args):
                     "bit_identical": bool(diffs) and all(np.array_equal(e2e_pose[k], plain_pose[k]) for k in both),
                     "basis": "camera->world pose of each of the first sessions after the same frame, from the "
                              "pipelined batch of all sessions (e2e leg) and from the plain one-session path"}
+
+    # config-5 serving in real time, every other leg's sessions released
+    torch.cuda.synchronize()
+    serving = serve_run(L, K, args.serve_seconds, shape.get("groups") or args.groups, stream) \
+        if args.serve_seconds > 0 else None
 
     prec_frames = host_frames(L, K, args.precision_frames, seed=replica_seeds(rank, S)[0]) \
         if args.precision_frames > 0 and rank == 0 else None
@@ -950,7 +997,7 @@ def scale_config(L):
     return L.default_config(voxel_size=0.005, truncation=0.02, zmin_update=0.3, zmax_update=4.0, zmin_raycast=0.3,
                             zmax_raycast=4.0, num_buckets=1 << 21, num_blocks=1 << 20,
                             voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3, max_iterations=[10, 5, 3, 3, 3],
-                            w_icp=1.0, w_rgb=0.1, max_probe=1024)
+                            w_rgb=0.1, max_probe=1024, motion_prior=1)
 
 
 def phase_bytes(phase: str, P: int, levels: int, s_v: int, d: dict) -> float | None:
@@ -1095,7 +1142,10 @@ def run_scale(args):
                                f"(0.5 m/s, 30 fps) in an 8x8x3 m room with 20 spheres and 12 boxes",
                    "voxel_m": cfg.voxel_size, "truncation_m": cfg.truncation, "hash_slots": 1 << 21,
                    "pool_blocks": 1 << 20, "voxel_layout": LAYOUTS[LAYOUT][1], "w_icp": cfg.w_icp,
-                   "w_rgb": cfg.w_rgb, "pyramid": "3 levels 10/5/3", "mesh_every": SCALE_MESH_EVERY},
+                   "w_rgb": cfg.w_rgb, "pyramid": "3 levels 10/5/3", "mesh_every": SCALE_MESH_EVERY,
+                   "motion_prior": "constant velocity: each frame's tracking starts from the last frame's motion "
+                                   "(at 16.7 mm per frame the reference's no-motion start is beyond its 1 cm ICP "
+                                   "gate; over 2000 frames it lost the camera from frame 1274 in a measured run)"},
         "latency_ms": {"p50": q(0.5), "p99": q(0.99), "basis": "CUDA events around each frame's gbf_process_frame"},
         "mesh_ms_total": sum(mesh_ms),
         "phases": phases, "peak_gbs": peak, "peak_source": f"{peak_kind} hbm_gbs",

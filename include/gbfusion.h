@@ -121,6 +121,9 @@ typedef struct gbf_config {
     float icp_angle_thresh; /* compared with |n_c x n_l| (reference cos(30*3.14/180)) */
     int32_t bilateral;    /* 1: bilateral-filter the tracking depth (reference)   */
     int32_t max_probe;    /* hash probe limit (bounded insert/lookup)             */
+    int32_t motion_prior; /* 0: a frame's tracking starts from no motion (the reference,
+                             rgbd_odometry.cpp:33-37); 1: from the last frame's motion
+                             when that frame tracked (constant velocity), else none  */
 } gbf_config;
 
 typedef struct gbf_track_result {
@@ -361,6 +364,15 @@ GBF_API gbf_status gbf_batch_create(int32_t max_sessions, gbf_batch **out);
  * cannot outlive the batch). */
 GBF_API gbf_status gbf_batch_destroy(gbf_batch *b);
 GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s);
+/* No counterpart in the reference (one map per process there).  Reserve the
+ * tick's shape for up to `slots` slots of sessions no larger than (cfg, K):
+ * frame size, pyramid, iteration counts, block pool and voxel layout.  The
+ * captured tick depends only on that shape, so with a reservation, sessions
+ * of up to that size put into and taken out of slots below `slots` (serving
+ * admission and eviction) keep the captured graphs and the tuner's choice;
+ * launches are sized for the reservation, and smaller sessions' surplus
+ * CTAs return at once.  slots = 0 drops the reservation. */
+GBF_API gbf_status gbf_batch_reserve(gbf_batch *b, const gbf_config *cfg, const gbf_intrinsics *K, int32_t slots);
 /* One frame for every slot with active[slot] != 0, from each session's staging
  * buffers, all sessions in the same launches; replayed from a CUDA graph when
  * use_graph != 0 (captured on first use for the current slot assignment). */

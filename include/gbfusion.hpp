@@ -214,6 +214,11 @@ class FusionBatch {
         check(gbf_batch_set(handle(), slot, s ? s->handle() : nullptr), "FusionBatch::set");
         held_.at(slot) = s ? s->shared_handle() : nullptr;
     }
+    // size the tick for `slots` sessions no larger than (cfg, K): sessions of up
+    // to that size then come and go without a new captured graph
+    void reserve(const gbf_config &cfg, const gbf_intrinsics &K, int slots) {
+        check(gbf_batch_reserve(handle(), &cfg, &K, slots), "FusionBatch::reserve");
+    }
     // frames read from device memory at each tick (nullptr, nullptr: the session's staging)
     void set_inputs(int slot, const uint16_t *depth_dev, const uint8_t *rgb_dev) {
         check(gbf_batch_set_inputs(handle(), slot, depth_dev, rgb_dev), "FusionBatch::set_inputs");

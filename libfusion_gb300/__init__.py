@@ -341,6 +341,12 @@ class FusionBatch:
         call("gbf_batch_set", self._h, slot, session.handle if session is not None else None)
         self.slots[slot] = session
 
+    def reserve(self, K: IntrinsicMatrix, cfg: _lib.Config, slots: int) -> None:
+        """Size the tick for `slots` sessions no larger than (K, cfg), so that
+        sessions of up to that size come and go without a new captured graph."""
+        kc = K.c()
+        call("gbf_batch_reserve", self._h, C.byref(cfg), C.byref(kc), slots)
+
     def set_inputs(self, slot: int, depth_ptr: int | None, rgb_ptr: int | None) -> None:
         """Take slot's next frame from these device pointers (dense u16, rgb8)."""
         call("gbf_batch_set_inputs", self._h, slot, depth_ptr, rgb_ptr)

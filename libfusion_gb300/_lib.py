@@ -41,7 +41,7 @@ class Config(C.Structure):
         ("num_levels", C.c_int32), ("max_iterations", C.c_int32 * MAX_LEVELS),
         ("w_icp", C.c_float), ("w_rgb", C.c_float),
         ("icp_dist_thresh", C.c_float), ("icp_angle_thresh", C.c_float),
-        ("bilateral", C.c_int32), ("max_probe", C.c_int32),
+        ("bilateral", C.c_int32), ("max_probe", C.c_int32), ("motion_prior", C.c_int32),
     ]
 
 
@@ -143,6 +143,7 @@ SIGNATURES = {
     "gbf_batch_create": (C.c_int, [_I32, C.POINTER(_P)]),
     "gbf_batch_destroy": (C.c_int, [_P]),
     "gbf_batch_set": (C.c_int, [_P, _I32, _P]),
+    "gbf_batch_reserve": (C.c_int, [_P, C.POINTER(Config), C.POINTER(Intrinsics), _I32]),
     "gbf_batch_process": (C.c_int, [_P, _P, _I32, _P]),
     "gbf_batch_set_inputs": (C.c_int, [_P, _I32, _P, _P]),
     "gbf_batch_set_timing": (C.c_int, [_P, _I32]),

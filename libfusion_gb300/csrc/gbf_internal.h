@@ -109,4 +109,9 @@ struct gbf_batch {
     std::vector<std::vector<float>> tune_ms;  // tick times (ms) per candidate
     cudaEvent_t tev[2][2] = {};         // per tick parity: start, end of the tick
     int tick_cand[2] = {-1, -1};        // candidate the tick in flight was timed for
+    // reserved shape (gbf_batch_reserve): the tick's extents and slot count never
+    // fall below these, so sessions up to it come and go without a new graph
+    gbf::Extent floor_ex{};
+    int floor_slots = 0;
+    int floor_layouts[gbf::kNumLayouts] = {};
 };

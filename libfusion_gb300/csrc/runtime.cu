@@ -69,6 +69,7 @@ gbf_status validate(const gbf_config *c, const gbf_intrinsics *K) {
     if (c->voxel_layout < 0 || c->voxel_layout >= kNumLayouts)
         return set_error(GBF_ERR_INVALID_ARG, "unknown voxel layout");
     if (c->max_probe < 1) return set_error(GBF_ERR_INVALID_ARG, "max_probe must be >= 1");
+    if (c->motion_prior != 0 && c->motion_prior != 1) return set_error(GBF_ERR_INVALID_ARG, "motion_prior must be 0 or 1");
     for (int l = 0; l < c->num_levels; ++l)
         if (c->max_iterations[l] < 0 || c->max_iterations[l] > 1000)
             return set_error(GBF_ERR_INVALID_ARG, "max_iterations out of range");
@@ -409,6 +410,7 @@ GBF_API gbf_status gbf_session_create(const gbf_config *cfg, const gbf_intrinsic
     v.cap_mask = (cfg->num_buckets & (cfg->num_buckets - 1)) == 0 ? cfg->num_buckets - 1 : -1;
     v.pool = cfg->num_blocks;
     v.max_probe = cfg->max_probe;
+    v.motion_prior = cfg->motion_prior;
     v.voxel = cfg->voxel_size;
     v.inv_voxel = 1.0f / cfg->voxel_size;                         // MapState::inverse_voxel_size
     v.tau = cfg->truncation;
@@ -1010,6 +1012,8 @@ GBF_API gbf_status gbf_batch_destroy(gbf_batch *b) {
     return check_cuda("gbf_batch_destroy");
 }
 
+static void batch_reshape(gbf_batch *b);
+
 GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
     if (!b || slot < 0 || slot >= b->max_slots) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_set: bad slot");
     std::lock_guard<std::mutex> lock(b->mu);
@@ -1020,9 +1024,15 @@ GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
         if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
     b->sessions[slot] = s;
     b->staged[0][slot] = b->staged[1][slot] = 0;
-    int nslots = 0, layouts[kNumLayouts] = {};
-    Extent ex;
-    memset(&ex, 0, sizeof(ex));
+    batch_reshape(b);
+    return GBF_OK;
+}
+
+// The tick's shape: the reserved floor, raised by the sessions in the slots.
+static void batch_reshape(gbf_batch *b) {
+    int nslots = b->floor_slots, layouts[kNumLayouts] = {};
+    for (int i = 0; i < kNumLayouts; ++i) layouts[i] = b->floor_layouts[i];
+    Extent ex = b->floor_ex;
     for (int i = 0; i < b->max_slots; ++i) {
         gbf_session *t = b->sessions[i];
         if (!t) continue;
@@ -1051,6 +1061,37 @@ GBF_API gbf_status gbf_batch_set(gbf_batch *b, int32_t slot, gbf_session *s) {
     b->nslots = nslots;
     b->ex = ex;
     memcpy(b->layouts, layouts, sizeof(layouts));
+}
+
+GBF_API gbf_status gbf_batch_reserve(gbf_batch *b, const gbf_config *cfg, const gbf_intrinsics *K, int32_t slots) {
+    if (!b || slots < 0 || slots > b->max_slots) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_reserve: bad slots");
+    if (slots > 0) {
+        gbf_status st = validate(cfg, K);
+        if (st != GBF_OK) return st;
+    }
+    std::lock_guard<std::mutex> lock(b->mu);
+    gbf_status fs = batch_flush(b, nullptr);
+    if (fs != GBF_OK) return fs;
+    for (int k = 0; k < 2; ++k)
+        if (b->ev_used[k]) cudaEventSynchronize(b->ev[k]);
+    Extent ex;
+    memset(&ex, 0, sizeof(ex));
+    memset(b->floor_layouts, 0, sizeof(b->floor_layouts));
+    if (slots > 0) {  // the extents gbf_session_create gives a session of (cfg, K)
+        ex.w = K->width;
+        ex.h = K->height;
+        ex.max_pool = cfg->num_blocks;
+        ex.levels = cfg->num_levels;
+        for (int l = 0; l < cfg->num_levels; ++l) {
+            const int pw = K->width >> l, ph = K->height >> l, tile = reduce_tile(l);
+            ex.max_red[l] = std::max(1, (pw * ph + tile - 1) / tile);
+            ex.max_iter[l] = cfg->max_iterations[l];
+        }
+        b->floor_layouts[cfg->voxel_layout] = 1;
+    }
+    b->floor_ex = ex;
+    b->floor_slots = slots;
+    batch_reshape(b);
     return GBF_OK;
 }
 

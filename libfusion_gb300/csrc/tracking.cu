@@ -707,6 +707,12 @@ __global__ void track_finish_kernel(const SessionView *__restrict__ svs, int fra
         pose_identity(ts->update);
     }
     if (frame_mode) {
+        // the next frame's initial estimate: no motion (the reference), or
+        // with the constant-velocity prior the motion this frame tracked
+        if (sv.motion_prior && ts->tracking && ts->success)
+            pose_inverse(ts->update, ts->init);
+        else
+            pose_identity(ts->init);
         ts->idx = 1 - ts->idx;
         ts->has_ref = 1;
         pose_copy(ts->pose, ts->map_pose);

@@ -45,6 +45,7 @@ typedef struct or_config {
     int32_t max_iterations[OR_MAX_LEVELS];
     float w_icp, w_rgb, icp_dist_thresh, icp_angle_thresh;
     int32_t bilateral;
+    int32_t motion_prior;     /* 1: track from the last frame's motion (constant velocity) */
     int32_t threads;          /* OpenMP threads, 0 = default */
 } or_config;
 

@@ -24,7 +24,8 @@ class OrConfig(C.Structure):
         ("num_blocks", C.c_int32), ("voxel_layout", C.c_int32), ("num_levels", C.c_int32),
         ("max_iterations", C.c_int32 * MAX_LEVELS),
         ("w_icp", C.c_float), ("w_rgb", C.c_float), ("icp_dist_thresh", C.c_float),
-        ("icp_angle_thresh", C.c_float), ("bilateral", C.c_int32), ("threads", C.c_int32),
+        ("icp_angle_thresh", C.c_float), ("bilateral", C.c_int32), ("motion_prior", C.c_int32),
+        ("threads", C.c_int32),
     ]
 
 

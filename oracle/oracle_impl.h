@@ -1289,6 +1289,7 @@ struct SFX(or_system) {
     FRAME *fr[2];
     int ref, has_ref;
     double pose[12];
+    double prior[16];   /* the next frame's initial estimate (gbf_config::motion_prior) */
     or_track_result last;
     float *depth_m, *vmap;
 };
@@ -1302,6 +1303,7 @@ SYS *SFX(or_system_create)(const or_config *cfg, const or_intrinsics *K) {
     s->fr[0] = SFX(or_frame_create)(cfg, K);
     s->fr[1] = SFX(or_frame_create)(cfg, K);
     pose_eye(s->pose);
+    pose_eye(s->prior);
     s->depth_m = (float *)malloc((size_t)K->width * K->height * sizeof(float));
     s->vmap = (float *)malloc((size_t)K->width * K->height * 4 * sizeof(float));
     return s;
@@ -1337,8 +1339,7 @@ void SFX(or_process_frame)(SYS *s, const uint16_t *depth_mm, const uint8_t *rgb)
     const int cur = 1 - s->ref;
     SFX(or_build_pyramid)(s->fr[cur], s->depth_m, rgb);
     if (s->has_ref) {
-        double eye[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
-        SFX(or_track)(s->fr[s->ref], s->fr[cur], eye, &s->last);
+        SFX(or_track)(s->fr[s->ref], s->fr[cur], s->prior, &s->last);
         double np[12];
         pose_mul(s->pose, s->last.update, np);
         memcpy(s->pose, np, sizeof(np));
@@ -1346,6 +1347,12 @@ void SFX(or_process_frame)(SYS *s, const uint16_t *depth_mm, const uint8_t *rgb)
         memset(&s->last, 0, sizeof(s->last));
         s->last.success = 1;
     }
+    /* the next frame starts from no motion (rgbd_odometry.cpp:33-37), or with
+     * the constant-velocity prior from the motion this frame tracked */
+    if (s->cfg.motion_prior && s->has_ref && s->last.success)
+        pose_inv(s->last.update, s->prior);
+    else
+        pose_eye(s->prior);
     s->ref = cur;
     s->has_ref = 1;
     /* fuse the raw depth with the new frame's level-0 normals (voxel_hashing.cpp:44-65) */

@@ -41,6 +41,7 @@ def test_version_and_defaults(L):
     assert abs(c.zmax_update - 1.5) < 1e-7 and abs(c.zmin_update - 0.3) < 1e-7
     assert list(c.max_iterations)[:3] == [10, 5, 3]
     assert c.w_icp == 1e6 and c.w_rgb == 1.0
+    assert c.motion_prior == 0  # each frame starts from no motion, as DenseOdometry::trackFrame does
 
 
 def test_session_bytes_and_validation(L):
@@ -54,7 +55,7 @@ def test_session_bytes_and_validation(L):
     c.voxel_layout = L.VOXEL_SNORM  # same 8 B per voxel as HALF
     assert L.session_bytes(c, K) == half
     for bad in (dict(num_levels=0), dict(num_levels=6), dict(voxel_size=0.0), dict(num_blocks=0),
-                dict(voxel_layout=3), dict(voxel_layout=-1), dict(max_probe=0)):
+                dict(voxel_layout=3), dict(voxel_layout=-1), dict(max_probe=0), dict(motion_prior=2)):
         cb = L.default_config(**bad)
         with pytest.raises(L.GbfError):
             L.session_bytes(cb, K)

@@ -449,3 +449,80 @@ def test_batch_calls_from_several_threads(gbf):
         for x, y in zip(H.sort_blocks(*s.export()), H.sort_blocks(*alone.export())):
             assert np.array_equal(x, y)
     batch.close()
+
+
+def test_motion_prior_matches_oracle(gbf):
+    """With the constant-velocity prior (motion_prior = 1) each frame's
+    Gauss-Newton starts from the motion the last frame tracked; the GPU loop
+    follows the FP32 oracle's within the same bound as without it, on frames
+    two steps apart (faster motion)."""
+    import oracle as O
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 0, bilateral=0, motion_prior=1)
+    fr = H.frames(L, K, 10, step=2)
+    s, gp = _run_gpu(L, K, cfg, fr)
+    osys = O.OracleSystem(O.config_from(cfg), O.intrinsics_from(K))
+    osys.set_pose(fr[0][2])
+    ok = []
+    for d, c, T in fr:
+        osys.process(d, c)
+        ok.append(osys.last_result().success)
+    gp = np.array(gp)
+    assert np.abs(gp[-1, :3, 3] - osys.pose()[:3, 3]).max() < 1e-3
+    assert bool(s.stats().track.success) == bool(ok[-1])
+    truth = np.array([f[2] for f in fr])
+    assert np.abs(gp[:, :3, 3] - truth[:, :3, 3]).max() < 0.02
+
+
+def test_server_results_alone_and_in_the_mix(gbf):
+    """The continuous-batching server (libfusion_gb300/serving.py) on the GPU:
+    three requests of two voxel sizes through a two-slot batch whose memory
+    budget holds two session arenas.  The third request waits for a slot,
+    takes the memory of an evicted session, and every session's poses, frame
+    by frame, equal those of the same frames run alone on the plain path, bit
+    for bit, whatever else shared its ticks."""
+    import torch
+    from libfusion_gb300.serving import ArenaCache, Request, Server
+    L = gbf
+    K = H.intrinsics(L)
+    cfgs = {8: H.small_config(L, 2, voxel_size=0.008, truncation=0.024),
+            10: H.small_config(L, 2, voxel_size=0.01)}
+    nbytes = {v: L.session_bytes(c, K) for v, c in cfgs.items()}
+    spec = [(0, 0.0, 8, 12, 3), (1, 0.0, 10, 9, 4), (2, 0.02, 8, 10, 5)]  # sid, arrival, voxel mm, frames, seed
+    frames = {}
+    for sid, _, _, n, seed in spec:
+        sc = L.SynthScene(seed=seed)
+        d = torch.empty((n, K.height, K.width), dtype=torch.uint16, device="cuda")
+        c = torch.empty((n, K.height, K.width, 3), dtype=torch.uint8, device="cuda")
+        for k in range(n):
+            sc.render_into(K, k, d[k].data_ptr(), c[k].data_ptr())
+        frames[sid] = (d, c, sc.pose(0))
+        sc.close()
+    torch.cuda.synchronize()
+    batch = L.FusionBatch(2)
+    batch.reserve(K, cfgs[8], 2)
+    batch.set_groups(1)
+    cache = ArenaCache(nbytes[8] + nbytes[10], make=lambda key: L.System(K, cfgs[key[0]]),
+                       destroy=lambda s: s.close(), reset=lambda s: s.reset())
+    srv = Server(batch, 2, cache, record_poses=True)
+    for sid, t, v, n, _ in spec:
+        d, c, T0 = frames[sid]
+        srv.submit(Request(sid=sid, arrival=t, frames=n, key=(v,), nbytes=nbytes[v], pose0=T0, fps=200.0,
+                           source=lambda k, d=d, c=c: (d[k].data_ptr(), c[k].data_ptr())))
+    srv.run(10.0)
+    rep = srv.report()
+    assert rep["completed"] == 3 and rep["frames"] == sum(n for _, _, _, n, _ in spec)
+    assert rep["deferred_by_slots"] >= 1 and rep["concurrency_peak"] == 2
+    assert rep["memory"]["peak_bytes"] <= nbytes[8] + nbytes[10]
+    assert rep["tracking_failed_frames"] == 0
+    batch.close()
+    cache.close()
+    for sid, _, v, n, _ in spec:
+        d, c, T0 = frames[sid]
+        s = L.System(K, cfgs[v])
+        s.set_pose(T0)
+        for k in range(n):
+            s.process_images(d[k], c[k])
+            assert np.array_equal(s.get_camera_pose(), srv.poses[(sid, k)]), (sid, k)
+        s.close()
