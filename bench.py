@@ -42,6 +42,7 @@ LAYOUTS = {"half": (1, "fp16 sdf + binary16 weight + rgba8 (8 B/voxel)"),
            "ref": (0, "int16 sdf (truncated) + f32 weight + rgba8 (12 B/voxel)")}
 LAYOUT = "snorm"  # the 8-byte layout within the 1e-3 x truncation TSDF error goal (HALF's fp16 step is not)
 PREC_FRAMES = 20  # frames of the precision check (tracking loop and mapping at ground-truth poses)
+MARCH_SKIP = 1    # the raycast crosses an unallocated block in one step (gbf_config::march_skip)
 
 
 def parse():
@@ -61,6 +62,9 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=40.0,
                     help="wall-clock seconds of the continuous-batching serving run (0: skip)")
     ap.add_argument("--layout", default="snorm", choices=sorted(LAYOUTS), help="voxel storage of every session")
+    ap.add_argument("--march-skip", type=int, default=MARCH_SKIP, choices=[0, 1],
+                    help="1: the raycast crosses a block that is not allocated in one step (0: the reference's "
+                         "2-voxel steps)")
     ap.add_argument("--precision-frames", type=int, default=PREC_FRAMES,
                     help="frames of the precision check against the FP64 oracle (0: skip)")
     ap.add_argument("--workload", default="served", choices=["served", "mixed", "scale"],
@@ -78,13 +82,14 @@ def session_config(L, i: int):
     tau = min(max(3.0 * v, 0.02), 0.03)
     return L.default_config(voxel_size=v, truncation=tau, zmin_update=0.3, zmax_update=4.0, zmin_raycast=0.3,
                             zmax_raycast=4.0, num_buckets=1 << 19, num_blocks=1 << 18, voxel_layout=LAYOUTS[LAYOUT][0],
-                            num_levels=3, max_iterations=[10, 5, 3, 3, 3], max_probe=256)
+                            num_levels=3, max_iterations=[10, 5, 3, 3, 3], max_probe=256, march_skip=MARCH_SKIP)
 
 
 def workload_config(sessions: int) -> dict:
     """The served workload both arms report."""
     return {"workload": f"served: {sessions} concurrent 640x480 sessions per GPU, one frame each per tick",
             "sessions_per_gpu": sessions, "voxel_m": list(VOXELS), "truncation": "clip(3*voxel, 2 cm, 3 cm)",
+            "march": "unallocated blocks crossed in one step" if MARCH_SKIP else "the reference's 2-voxel steps",
             "voxel_layout": LAYOUTS[LAYOUT][1], "pool_blocks": 1 << 18,
             "hash_slots": 1 << 19, "pyramid": "3 levels 10/5/3"}
 
@@ -498,7 +503,7 @@ def serve_config(L, v_mm: int):
     return L.default_config(voxel_size=v, truncation=min(max(3.0 * v, 0.02), 0.03), zmin_update=0.3,
                             zmax_update=4.0, zmin_raycast=0.3, zmax_raycast=4.0, num_buckets=2 * pool,
                             num_blocks=pool, voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3,
-                            max_iterations=[10, 5, 3, 3, 3], max_probe=256)
+                            max_iterations=[10, 5, 3, 3, 3], max_probe=256, march_skip=MARCH_SKIP)
 
 
 def serve_run(L, K, seconds: float, groups: int, stream, rate: float = 4.0, slots: int = 64,
@@ -895,7 +900,7 @@ def mixed_session(L, i):
     cfg = L.default_config(voxel_size=v, truncation=min(max(3.0 * v, 0.02), 0.05), zmin_update=0.3,
                            zmax_update=4.0, zmin_raycast=0.3, zmax_raycast=4.0, num_buckets=1 << 19,
                            num_blocks=1 << 18, voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3,
-                           max_iterations=[10, 5, 3, 3, 3], max_probe=256)
+                           max_iterations=[10, 5, 3, 3, 3], max_probe=256, march_skip=MARCH_SKIP)
     return K, cfg
 
 
@@ -997,7 +1002,7 @@ def scale_config(L):
     return L.default_config(voxel_size=0.005, truncation=0.02, zmin_update=0.3, zmax_update=4.0, zmin_raycast=0.3,
                             zmax_raycast=4.0, num_buckets=1 << 21, num_blocks=1 << 20,
                             voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3, max_iterations=[10, 5, 3, 3, 3],
-                            w_rgb=0.1, max_probe=1024, motion_prior=1)
+                            w_rgb=0.1, max_probe=1024, motion_prior=1, march_skip=MARCH_SKIP)
 
 
 def phase_bytes(phase: str, P: int, levels: int, s_v: int, d: dict) -> float | None:
@@ -1040,7 +1045,7 @@ def run_scale(args):
     torch.cuda.set_stream(stream)
     bufs = [(torch.empty((H, W), dtype=torch.uint16, device="cuda"),
              torch.empty((H, W, 3), dtype=torch.uint8, device="cuda")) for _ in range(2)]
-    max_tris = 1 << 24
+    max_tris = 1 << 25  # 1.2 GB of vertices: the 2000-frame map meshes to over 2^24 triangles
     vtx = torch.empty((max_tris, 3, 3), dtype=torch.float32, device="cuda")
     truth = [sc.pose(k) for k in range(n)]
 
@@ -1158,9 +1163,10 @@ def run_scale(args):
 
 
 def main():
-    global LAYOUT
+    global LAYOUT, MARCH_SKIP
     args = parse()
     LAYOUT = args.layout
+    MARCH_SKIP = args.march_skip
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "mixed":

@@ -27,7 +27,7 @@ struct ArenaLayout {
     size_t table, bcoord, bstamp, bfresh, vis, mesh_off, vox_sw, vox_rgb, ctr, ts;
     size_t in_depth, in_rgb, depth_raw, rgb4, nmap_ext, fuse_px, zr_min, zr_max, partials;
     size_t depth[kMaxLevels], inten[2][kMaxLevels], gx[kMaxLevels], gy[kMaxLevels];
-    size_t vmap[2][kMaxLevels], nmap[2][kMaxLevels];
+    size_t vmap[2][kMaxLevels], nmap[2][kMaxLevels], igd[2][kMaxLevels];
 };
 
 gbf_status validate(const gbf_config *cfg, const gbf_intrinsics *K);

@@ -89,6 +89,7 @@ struct SessionView {
     int layout;            // gbf_voxel_layout
     int cap, pool, max_probe;
     int motion_prior;      // gbf_config::motion_prior
+    int march_skip;        // gbf_config::march_skip
     int cap_mask;          // cap - 1 when cap is a power of two, else -1
     float voxel, inv_voxel, tau, inv_tau, step_scale;
     float zmin_u, zmax_u, zmin_r, zmax_r, block_metric;
@@ -122,6 +123,9 @@ struct SessionView {
     float *inten[2][kMaxLevels];
     float *gx[kMaxLevels];
     float *gy[kMaxLevels];
+    // per set and level, (I, dI/dx, dI/dy, 0) of each pixel: one 16-byte gather per
+    // bilinear tap of the photometric row instead of three 4-byte ones (null: not kept)
+    float4 *igd[2][kMaxLevels];
     float4 *vmap[2][kMaxLevels];
     float4 *nmap[2][kMaxLevels];
     float *zr_min, *zr_max;

@@ -186,8 +186,11 @@ __global__ void __launch_bounds__(256, 8) level_maps_kernel(const SessionView *_
     const float nanf_ = __int_as_float(0x7fffffff);
     if (x < K.w - 1 && y < K.h - 1) {
         const int x10 = max(x - 1, 0), y10 = max(y - 1, 0);
-        sv.gx[level][i] = (I[(size_t)y * K.w + x + 1] - I[(size_t)y * K.w + x10]) * 0.5f;
-        sv.gy[level][i] = (I[(size_t)(y + 1) * K.w + x] - I[(size_t)y10 * K.w + x]) * 0.5f;
+        const float gx = (I[(size_t)y * K.w + x + 1] - I[(size_t)y * K.w + x10]) * 0.5f;
+        const float gy = (I[(size_t)(y + 1) * K.w + x] - I[(size_t)y10 * K.w + x]) * 0.5f;
+        sv.gx[level][i] = gx;
+        sv.gy[level][i] = gy;
+        sv.igd[set][level][i] = make_float4(I[i], gx, gy, 0.f);
         const float4 v00 = back_project(D, K.w, x10, y, K);
         const float4 v01 = back_project(D, K.w, x + 1, y, K);
         const float4 v10 = back_project(D, K.w, x, y10, K);
@@ -199,6 +202,7 @@ __global__ void __launch_bounds__(256, 8) level_maps_kernel(const SessionView *_
         // the reference leaves the last row / column unwritten; write invalid
         sv.gx[level][i] = 0.f;
         sv.gy[level][i] = 0.f;
+        sv.igd[set][level][i] = make_float4(I[i], 0.f, 0.f, 0.f);
         sv.nmap[set][level][i] = make_float4(nanf_, nanf_, nanf_, nanf_);
         if (level == 0 && set_sel == 0) fuse_weight(sv, i, make_float4(nanf_, nanf_, nanf_, nanf_));
     }

@@ -229,6 +229,20 @@ __device__ __forceinline__ float interp2(const float *img, int w, float x, float
     return (r0[u] * (1.0f - ax) + r0[u + 1] * ax) * (1.0f - ay) + (r1[u] * (1.0f - ax) + r1[u + 1] * ax) * ay;
 }
 
+// interp2 of the intensity and both gradients at once from the packed
+// (I, dI/dx, dI/dy, 0) image: four 16-byte taps, each channel the same
+// expression as interp2.
+__device__ __forceinline__ float3 interp2_igd(const float4 *img, int w, float x, float y) {
+    const int u = (int)floorf(x), v = (int)floorf(y);
+    const float ax = x - (float)u, ay = y - (float)v;
+    const float4 *r0 = img + (size_t)v * w, *r1 = r0 + w;
+    const float4 a = r0[u], b = r0[u + 1], c = r1[u], d = r1[u + 1];
+    const float bx = 1.0f - ax, by = 1.0f - ay;
+    return make_float3((a.x * bx + b.x * ax) * by + (c.x * bx + d.x * ax) * ay,
+                       (a.y * bx + b.y * ax) * by + (c.y * bx + d.y * ax) * ay,
+                       (a.z * bx + b.z * ax) * by + (c.z * bx + d.z * ax) * ay);
+}
+
 // ICPReduction::searchPoint + getRow (pose_estimator.cu:168-222)
 __device__ __forceinline__ bool icp_row(const SessionView &sv, int level, int cs, const M34 &T, const float4 vl,
                                         const float4 nl4, float row[7]) {
@@ -273,7 +287,10 @@ __device__ __forceinline__ PhotoConst photo_const(float stddev) {
     return c;
 }
 
-// RgbReduction2::find_corresp + compute_jacobian (m_estimator.cu:315-391)
+// RgbReduction2::find_corresp + compute_jacobian (m_estimator.cu:315-391).
+// PACKED: the current frame's intensity and gradients from its packed image
+// (sessions); otherwise from the three separate images (caller-owned images).
+template <bool PACKED>
 __device__ __forceinline__ bool rgb_row(const SessionView &sv, int level, int cs, const M34 &T,
                                         const PhotoConst &pc, const float4 pt, const float il, float row[7]) {
     const float stddev = pc.stddev;
@@ -284,9 +301,17 @@ __device__ __forceinline__ bool rgb_row(const SessionView &sv, int level, int cs
     const float u0 = (q.x / q.z) * K.fx + K.cx;
     const float v0 = (q.y / q.z) * K.fy + K.cy;
     if (!(u0 >= 2 && u0 < (float)(K.w - 2) && v0 >= 2 && v0 < (float)(K.h - 2))) return false;
-    const float ic = interp2(sv.inten[cs][level], K.w, u0, v0);
-    const float dx = interp2(sv.gx[level], K.w, u0, v0);
-    const float dy = interp2(sv.gy[level], K.w, u0, v0);
+    float ic, dx, dy;
+    if (PACKED) {
+        const float3 g = interp2_igd(sv.igd[cs][level], K.w, u0, v0);
+        ic = g.x;
+        dx = g.y;
+        dy = g.z;
+    } else {
+        ic = interp2(sv.inten[cs][level], K.w, u0, v0);
+        dx = interp2(sv.gx[level], K.w, u0, v0);
+        dy = interp2(sv.gy[level], K.w, u0, v0);
+    }
     if (!((dx > 2 || dy > 2) && isfinite(ic) && isfinite(dx) && isfinite(dy))) return false;
     const float zi = __frcp_rn(q.z);  // float z_inv = 1.0 / z (same argument as icp_row)
     const float lx = (dx * K.fx) * zi, ly = (dy * K.fy) * zi;
@@ -378,6 +403,7 @@ struct ReduceSmem {
 // measured 1.4% slower over the track phase).  Warp
 // shuffle tree, then a fixed-order pass over the four warps of each half.
 // Writes 58 floats to part.
+template <bool PACKED>
 __device__ __forceinline__ void cta_partial(ReduceSmem &sm, const SessionView &sv, int level, int rs, int cs,
                                             const M34 &T, float stddev, int cta, int tile, float *part) {
     auto &warp_sums = sm.warp_sums;
@@ -430,7 +456,7 @@ __device__ __forceinline__ void cta_partial(ReduceSmem &sm, const SessionView &s
         if (c >= n) break;
         float row[7];
         const bool ok = half == 0 ? icp_row(sv, level, cs, T, s_v[c], s_n[c], row)
-                                  : rgb_row(sv, level, cs, T, pc, s_v[c], s_i[c], row);
+                                  : rgb_row<PACKED>(sv, level, cs, T, pc, s_v[c], s_i[c], row);
         if (ok) accumulate(acc, row);
     }
     const float total = warp_sum29(acc);
@@ -547,7 +573,7 @@ __global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const Sess
     __syncthreads();
     const int rs = ts->idx, cs = 1 - ts->idx;
     __shared__ ReduceSmem sm;
-    cta_partial(sm, sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.red_tile[level],
+    cta_partial<true>(sm, sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.red_tile[level],
                 sv.partials + (size_t)blockIdx.x * kPartialStride);
     __threadfence();
     __syncthreads();
@@ -826,7 +852,7 @@ __global__ void __launch_bounds__(kReduceThreads, 3) reduce_static_kernel(Sessio
         for (int i = 0; i < 12; ++i) T.m[i] = a.pose[i];
     __syncthreads();
     __shared__ ReduceSmem sm;
-    cta_partial(sm, sv, 0, 0, 1, T, a.stddev, blockIdx.x, kCtaPixels, scratch + (size_t)blockIdx.x * kPartialStride);
+    cta_partial<false>(sm, sv, 0, 0, 1, T, a.stddev, blockIdx.x, kCtaPixels, scratch + (size_t)blockIdx.x * kPartialStride);
     __threadfence();
     __syncthreads();
     __shared__ unsigned int ticket;

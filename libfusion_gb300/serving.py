@@ -34,7 +34,7 @@ from dataclasses import dataclass
 class Request:
     """A camera asking for a reconstruction session."""
     sid: int
-    arrival: float                 # seconds on the server's clock
+    arrival: float                 # seconds after the server starts
     frames: int                    # frames the camera will stream
     key: tuple                     # session configuration (arena reuse key)
     nbytes: int                    # device bytes of its session (gbf_session_bytes)
@@ -160,7 +160,7 @@ class Server:
 
     # ---------------------------------------------------------------- scheduling
     def _arrive(self, now: float) -> None:
-        while self.pending and self.pending[0].arrival <= now:
+        while self.pending and self.t0 + self.pending[0].arrival <= now:
             self.queue.append(self.pending.pop(0))
 
     def _admit(self, now: float) -> None:
@@ -189,7 +189,7 @@ class Server:
             slot = free[0]
             self.batch.set(slot, s)
             self.live[slot] = _Live(r, s, now)
-            self.queue_wait_s.append(now - r.arrival)
+            self.queue_wait_s.append(now - (self.t0 + r.arrival))
             n = sum(1 for x in self.live if x is not None)
             self.concurrency_peak = max(self.concurrency_peak, n)
 
@@ -207,13 +207,16 @@ class Server:
         """The earliest time something can happen: an arrival or a frame."""
         ts = [self._frame_time(x, x.next_frame) for x in self.live if x is not None]
         if self.pending:
-            ts.append(self.pending[0].arrival)
+            ts.append(self.t0 + self.pending[0].arrival)
         return min(ts) if ts else None
 
     def step(self) -> bool:
         """One round: arrivals, admissions, then one tick over the sessions with
-        a frame waiting.  Returns whether a tick ran."""
+        a frame waiting.  Returns whether a tick ran.  The first call starts
+        the server's clock, from which request arrivals count."""
         now = self.clock.now()
+        if self.t0 is None:
+            self.t0 = now
         self._arrive(now)
         self._admit(now)
         ready = [i for i, x in enumerate(self.live)

@@ -153,3 +153,18 @@ def test_eviction_empties_the_slot_and_resets_the_arena():
     assert batch.slots[0] is None
     arena = srv.cache.free[("a",)][0][0]
     assert arena.resets == 2  # reset when each session was evicted
+
+
+def test_arrivals_count_from_the_server_start():
+    """Request arrival times are seconds after the server starts, whatever the
+    clock reads then."""
+    srv, clock, _ = server(slots=4, budget=100)
+    clock.t = 1000.0
+    srv.submit(req(0, 0.0, frames=3))
+    srv.submit(req(1, 5.0, frames=3))
+    srv.run(1.0)
+    r = srv.report()
+    assert r["admitted"] == 1 and r["requests_arrived"] == 1
+    srv.run(6.0)
+    r = srv.report()
+    assert r["admitted"] == 2 and r["queue_wait_s"]["max"] < 0.1
