@@ -42,7 +42,6 @@ LAYOUTS = {"half": (1, "fp16 sdf + binary16 weight + rgba8 (8 B/voxel)"),
            "ref": (0, "int16 sdf (truncated) + f32 weight + rgba8 (12 B/voxel)")}
 LAYOUT = "snorm"  # the 8-byte layout within the 1e-3 x truncation TSDF error goal (HALF's fp16 step is not)
 PREC_FRAMES = 20  # frames of the precision check (tracking loop and mapping at ground-truth poses)
-MARCH_SKIP = 1    # the raycast crosses an unallocated block in one step (gbf_config::march_skip)
 
 
 def parse():
@@ -62,16 +61,14 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=40.0,
                     help="wall-clock seconds of the continuous-batching serving run (0: skip)")
     ap.add_argument("--layout", default="snorm", choices=sorted(LAYOUTS), help="voxel storage of every session")
-    ap.add_argument("--march-skip", type=int, default=MARCH_SKIP, choices=[0, 1],
-                    help="1: the raycast crosses a block that is not allocated in one step (0: the reference's "
-                         "2-voxel steps)")
     ap.add_argument("--precision-frames", type=int, default=PREC_FRAMES,
                     help="frames of the precision check against the FP64 oracle (0: skip)")
-    ap.add_argument("--workload", default="served", choices=["served", "mixed", "scale"],
+    ap.add_argument("--workload", default="served", choices=["served", "mixed", "scale", "precision"],
                     help="mixed: sessions of three resolutions and three voxel sizes in one batch "
                          "(served vs plain only; prints its own line); scale: the large-map "
                          "configuration as one plain session, phase by phase")
     ap.add_argument("--scale-frames", type=int, default=2000, help="frames of the scale workload")
+    ap.add_argument("--precision-track", type=int, default=2000, help="tracked frames of the precision workload")
     return ap.parse_args()
 
 
@@ -82,14 +79,13 @@ def session_config(L, i: int):
     tau = min(max(3.0 * v, 0.02), 0.03)
     return L.default_config(voxel_size=v, truncation=tau, zmin_update=0.3, zmax_update=4.0, zmin_raycast=0.3,
                             zmax_raycast=4.0, num_buckets=1 << 19, num_blocks=1 << 18, voxel_layout=LAYOUTS[LAYOUT][0],
-                            num_levels=3, max_iterations=[10, 5, 3, 3, 3], max_probe=256, march_skip=MARCH_SKIP)
+                            num_levels=3, max_iterations=[10, 5, 3, 3, 3], max_probe=256)
 
 
 def workload_config(sessions: int) -> dict:
     """The served workload both arms report."""
     return {"workload": f"served: {sessions} concurrent 640x480 sessions per GPU, one frame each per tick",
             "sessions_per_gpu": sessions, "voxel_m": list(VOXELS), "truncation": "clip(3*voxel, 2 cm, 3 cm)",
-            "march": "unallocated blocks crossed in one step" if MARCH_SKIP else "the reference's 2-voxel steps",
             "voxel_layout": LAYOUTS[LAYOUT][1], "pool_blocks": 1 << 18,
             "hash_slots": 1 << 19, "pyramid": "3 levels 10/5/3"}
 
@@ -503,7 +499,7 @@ def serve_config(L, v_mm: int):
     return L.default_config(voxel_size=v, truncation=min(max(3.0 * v, 0.02), 0.03), zmin_update=0.3,
                             zmax_update=4.0, zmin_raycast=0.3, zmax_raycast=4.0, num_buckets=2 * pool,
                             num_blocks=pool, voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3,
-                            max_iterations=[10, 5, 3, 3, 3], max_probe=256, march_skip=MARCH_SKIP)
+                            max_iterations=[10, 5, 3, 3, 3], max_probe=256)
 
 
 def serve_run(L, K, seconds: float, groups: int, stream, rate: float = 4.0, slots: int = 64,
@@ -900,7 +896,7 @@ def mixed_session(L, i):
     cfg = L.default_config(voxel_size=v, truncation=min(max(3.0 * v, 0.02), 0.05), zmin_update=0.3,
                            zmax_update=4.0, zmin_raycast=0.3, zmax_raycast=4.0, num_buckets=1 << 19,
                            num_blocks=1 << 18, voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3,
-                           max_iterations=[10, 5, 3, 3, 3], max_probe=256, march_skip=MARCH_SKIP)
+                           max_iterations=[10, 5, 3, 3, 3], max_probe=256)
     return K, cfg
 
 
@@ -1002,7 +998,7 @@ def scale_config(L):
     return L.default_config(voxel_size=0.005, truncation=0.02, zmin_update=0.3, zmax_update=4.0, zmin_raycast=0.3,
                             zmax_raycast=4.0, num_buckets=1 << 21, num_blocks=1 << 20,
                             voxel_layout=LAYOUTS[LAYOUT][0], num_levels=3, max_iterations=[10, 5, 3, 3, 3],
-                            w_rgb=0.1, max_probe=1024, motion_prior=1, march_skip=MARCH_SKIP)
+                            w_rgb=0.1, max_probe=1024, motion_prior=1)
 
 
 def phase_bytes(phase: str, P: int, levels: int, s_v: int, d: dict) -> float | None:
@@ -1162,17 +1158,159 @@ def run_scale(args):
     }), flush=True)
 
 
+def precision_config(L, layout: int):
+    """Config 1's map: 1 cm voxels, 3 cm truncation, 2^18 slots, 2^17-block pool."""
+    return L.default_config(voxel_size=0.01, truncation=0.03, zmin_update=0.3, zmax_update=4.0, zmin_raycast=0.3,
+                            zmax_raycast=4.0, num_buckets=1 << 18, num_blocks=1 << 17, voxel_layout=layout,
+                            num_levels=3, max_iterations=[10, 5, 3, 3, 3], max_probe=256)
+
+
+def trajectory_errors(poses, truth) -> dict:
+    """ATE (RMS of the camera position error) and RPE (RMS of the frame-to-frame
+    relative pose error: translation, rotation angle) against `truth`."""
+    P, T = np.asarray(poses), np.asarray(truth)
+    ate = np.sqrt(np.mean(np.sum((P[:, :3, 3] - T[:, :3, 3]) ** 2, axis=1)))
+    dt, dr = [], []
+    for k in range(1, len(P)):
+        e = np.linalg.inv(np.linalg.inv(T[k - 1]) @ T[k]) @ (np.linalg.inv(P[k - 1]) @ P[k])
+        dt.append(np.linalg.norm(e[:3, 3]))
+        dr.append(np.degrees(np.arccos(np.clip((np.trace(e[:3, :3]) - 1) / 2, -1, 1))))
+    return {"ate_mm": float(ate * 1e3), "rpe_mm": float(np.sqrt(np.mean(np.square(dt))) * 1e3),
+            "rpe_deg": float(np.sqrt(np.mean(np.square(dr)))), "max_error_mm":
+            float(np.max(np.linalg.norm(P[:, :3, 3] - T[:, :3, 3], axis=1)) * 1e3)}
+
+
+def run_precision(args):
+    """Config 3: the precision form of config 1 (the 4x4x3 m room, circle
+    path, 640x480), every voxel layout on the GPU against the FP64 oracle (the
+    checker, on the host cores).  The tracking loop runs --precision-track
+    frames (2000) on the GPU in each layout and in the FP64 oracle: trajectory
+    error against the ground truth (ATE, RPE), pose drift against the FP64
+    loop, tracking failures.  The map: --precision-frames frames fused at the
+    ground-truth poses with the normal-weighted update, then TSDF error, raycast
+    depth and the mesh's symmetric Chamfer distance against the FP64 map."""
+    import torch
+    import libfusion_gb300 as L
+    from libfusion_gb300 import build as B
+    B.build()
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    O.build()
+    from scipy.spatial import cKDTree
+    K = intrinsics(L)
+    n_track, n_map = args.precision_track, max(args.precision_frames, 2)
+    sc = L.SynthScene(seed=0)
+    truth = [sc.pose(k) for k in range(n_track)]
+    cu = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    threads = os.cpu_count() or 1
+    out = {"layouts": {}}
+    # ---- tracking loop, 2000 frames: GPU per layout, then the FP64 oracle on the same frames
+    fp64 = O.OracleSystem(O.config_from(precision_config(L, 0), threads=threads), O.intrinsics_from(K), "f64")
+    fp64.set_pose(truth[0])
+    gpu = {name: L.System(K, precision_config(L, LAYOUTS[name][0])) for name in LAYOUTS}
+    for s in gpu.values():
+        s.set_pose(truth[0])
+    gp = {name: [] for name in LAYOUTS}
+    gfail = {name: 0 for name in LAYOUTS}
+    op, ofail = [], 0
+    t0 = time.perf_counter()
+    t_oracle = 0.0
+    for k in range(n_track):
+        d, c = sc.render(K, k)
+        for name, s in gpu.items():
+            s.process_images(d, c)
+            gp[name].append(s.get_camera_pose())
+            gfail[name] += 0 if s.stats().track.success else 1
+        dh, ch = d.cpu().numpy(), c.cpu().numpy()
+        ta = time.perf_counter()
+        fp64.process(dh, ch)
+        t_oracle += time.perf_counter() - ta
+        op.append(fp64.pose())
+        ofail += 0 if fp64.last_result().success else 1
+    op = np.array(op)
+    out["fp64_oracle_tracking"] = dict(trajectory_errors(op, truth), failed_frames=ofail)
+    for name in LAYOUTS:
+        P = np.array(gp[name])
+        out["layouts"][name] = {"storage": LAYOUTS[name][1],
+                                "tracking": dict(trajectory_errors(P, truth), failed_frames=gfail[name],
+                                                 drift_vs_fp64_max_mm=float(np.abs(P[:, :3, 3] - op[:, :3, 3]).max()
+                                                                            * 1e3))}
+        gpu[name].close()
+    # ---- the map at the ground-truth poses (System's normal-weighted update)
+    om = O.OracleMap(O.config_from(precision_config(L, 0), threads=threads), O.intrinsics_from(K), "f64")
+    t = L.DenseTracking(K, precision_config(L, 0))
+    maps = {name: L.DenseMapping(K, precision_config(L, LAYOUTS[name][0])) for name in LAYOUTS}
+    for k in range(n_map):
+        d, c = sc.render(K, k)
+        dm = (d.float() * np.float32(0.001)).contiguous()
+        t.set_current(dm, c)
+        n = t.get_image(0, 1, 0)
+        for m in maps.values():
+            m.update(dm, c, truth[k], normal=n)
+        om.fuse(dm.cpu().numpy(), c.cpu().numpy(), truth[k], nmap=n.cpu().numpy())
+    T = truth[n_map - 1]
+    ov = om.raycast(T)
+    oc, osd, ow, _ = om.export()
+    okey = {tuple(x): i for i, x in enumerate(oc.tolist())}
+    ovtx, _ = om.mesh(0, 1 << 23)
+    otree = cKDTree(ovtx.reshape(-1, 3).astype(np.float64))
+    for name, m in maps.items():
+        gc, gs, gw, _ = m.export()
+        gi, oi = [], []
+        for i, x in enumerate(gc.tolist()):
+            j = okey.get(tuple(x))
+            if j is not None:
+                gi.append(i)
+                oi.append(j)
+        a, b, wa, wb = gs[gi], osd[oi], gw[gi], ow[oi]
+        both = (wa > 0) & (wb > 0)
+        err = np.abs(a[both] - b[both]).astype(np.float64)
+        vm = torch.full((K.height, K.width, 4), float("nan"), dtype=torch.float32, device="cuda")
+        m.raycast(vm, T)
+        gv = vm.cpu().numpy()
+        gh, oh = ~np.isnan(gv[..., 2]), ~np.isnan(ov[..., 2])
+        dz = np.abs(gv[..., 2][gh & oh] - ov[..., 2][gh & oh]).astype(np.float64)
+        same = dz < 0.03
+        vtx = torch.zeros((len(ovtx) + (1 << 16), 3, 3), dtype=torch.float32, device="cuda")
+        nt = m.fetch_mesh_vertex_only(vtx)
+        gpts = vtx[:nt].cpu().numpy().reshape(-1, 3).astype(np.float64)
+        d1, _ = otree.query(gpts)
+        d2, _ = cKDTree(gpts).query(otree.data)
+        out["layouts"][name]["map"] = {
+            "tsdf_err_over_tau": {"p99.9": float(np.quantile(err, 0.999)), "mean": float(err.mean()),
+                                  "max": float(err.max()), "voxels": int(both.sum())},
+            "raycast_depth_mm": {"same_surface_rms": float(np.sqrt(np.mean(dz[same] ** 2)) * 1e3),
+                                 "p99": float(np.quantile(dz[same], 0.99) * 1e3),
+                                 "hit_masks_differing": int(np.sum(gh != oh)), "other_surface": int(np.sum(~same))},
+            "mesh": {"triangles": int(nt), "fp64_triangles": int(len(ovtx)),
+                     "chamfer_mm": float((d1.mean() + d2.mean()) / 2 * 1e3),
+                     "hausdorff_mm": float(max(d1.max(), d2.max()) * 1e3)}}
+        m.close()
+    t.close()
+    sc.close()
+    print(json.dumps({
+        "metric": METRIC, "workload": "precision", "unit": "mm / fraction of truncation",
+        "config": {"workload": f"config-1 room (4x4x3 m, 6 spheres, 4 boxes, seed 0), circle path, 640x480: "
+                               f"{n_track} tracked frames, map of {n_map} frames at the ground-truth poses",
+                   "voxel_m": 0.01, "truncation_m": 0.03, "pyramid": "3 levels 10/5/3",
+                   "reference": "FP64 oracle (double arithmetic, unquantised voxels), host cores"},
+        "goals": {"pose_drift_mm": 1.0, "tsdf_p99.9_over_tau": 1e-3},
+        **out, "oracle_seconds": round(t_oracle, 1), "wall_s": round(time.perf_counter() - t0, 1),
+    }), flush=True)
+
+
 def main():
-    global LAYOUT, MARCH_SKIP
+    global LAYOUT
     args = parse()
     LAYOUT = args.layout
-    MARCH_SKIP = args.march_skip
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "mixed":
         run_mixed(args)
     elif args.workload == "scale":
         run_scale(args)
+    elif args.workload == "precision":
+        run_precision(args)
     else:
         run_ours(args)
 

@@ -124,10 +124,6 @@ typedef struct gbf_config {
     int32_t motion_prior; /* 0: a frame's tracking starts from no motion (the reference,
                              rgbd_odometry.cpp:33-37); 1: from the last frame's motion
                              when that frame tracked (constant velocity), else none  */
-    int32_t march_skip;   /* 0: the raycast steps 2 voxels at a time through a block that
-                             is not allocated (the reference, ray_tracing.cu:399-405);
-                             1: it jumps to its first 2-voxel step past that block in one
-                             step (the same samples up to the rounding of the position) */
 } gbf_config;
 
 typedef struct gbf_track_result {

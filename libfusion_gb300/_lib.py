@@ -42,7 +42,6 @@ class Config(C.Structure):
         ("w_icp", C.c_float), ("w_rgb", C.c_float),
         ("icp_dist_thresh", C.c_float), ("icp_angle_thresh", C.c_float),
         ("bilateral", C.c_int32), ("max_probe", C.c_int32), ("motion_prior", C.c_int32),
-        ("march_skip", C.c_int32),
     ]
 
 

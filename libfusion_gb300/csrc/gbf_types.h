@@ -89,7 +89,6 @@ struct SessionView {
     int layout;            // gbf_voxel_layout
     int cap, pool, max_probe;
     int motion_prior;      // gbf_config::motion_prior
-    int march_skip;        // gbf_config::march_skip
     int cap_mask;          // cap - 1 when cap is a power of two, else -1
     float voxel, inv_voxel, tau, inv_tau, step_scale;
     float zmin_u, zmax_u, zmin_r, zmax_r, block_metric;

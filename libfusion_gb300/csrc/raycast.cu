@@ -207,29 +207,6 @@ __device__ __forceinline__ float read_sdf_interped(const SV &sv, BlockCache &bc,
     return (1.0f - fz) * r2 + fz * r3;
 }
 
-// The march's step through an unallocated block (gbf_config::march_skip): the
-// reference steps 2 voxels at a time until a sample leaves the block
-// (ray_tracing.cu:399-405); this is the first multiple of 2 past the block's
-// exit, from the distance t to the nearest exit plane less 1e-3 voxel (so
-// rounding can only leave the sample inside the block, from where the next
-// step goes on).  IEEE divisions: the oracle computes the same step.
-__device__ __noinline__ float skip_step(float3 r, float3 dir, int bx, int by, int bz) {
-    const float inf = __int_as_float(0x7f800000);
-    const float tx = dir.x > 0.f ? ((float)((bx + 1) * 8) - r.x) / dir.x
-                   : dir.x < 0.f ? ((float)(bx * 8) - r.x) / dir.x : inf;
-    const float ty = dir.y > 0.f ? ((float)((by + 1) * 8) - r.y) / dir.y
-                   : dir.y < 0.f ? ((float)(by * 8) - r.y) / dir.y : inf;
-    const float tz = dir.z > 0.f ? ((float)((bz + 1) * 8) - r.z) / dir.z
-                   : dir.z < 0.f ? ((float)(bz * 8) - r.z) / dir.z : inf;
-    const float t = fminf(tx, fminf(ty, tz));  // under 14 voxels (a block's diagonal)
-    int k = 1;
-    if (t < 64.f) {
-        const int f = (int)floorf((t - 1e-3f) * 0.5f) + 1;
-        if (f > 1) k = f;
-    }
-    return (float)(2 * k);
-}
-
 // The fields the march reads on every step, copied into registers once per
 // thread: through the descriptor in global memory the compiler has to reload
 // them (the same copy took the integration from 2.29 to 1.76 ms).
@@ -302,7 +279,6 @@ __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionV
 
     const MarchView mv{sv.table, sv.vox_sw, sv.cap, sv.cap_mask, sv.max_probe};
     const float step_scale = sv.step_scale;
-    const bool skip = sv.march_skip != 0;
     BlockCache bc;
     bc.init();
     float sdf = 1.0f, last_sdf, step;
@@ -310,14 +286,10 @@ __global__ void __launch_bounds__(kRayThreads, 24) raycast_kernel(const SessionV
     for (int it = 0; dist_s < dist_e && it < kMaxMarch; ++it) {
         last_sdf = sdf;
         sdf = read_sdf<LAYOUT>(mv, bc, r.x, r.y, r.z, valid);
-        // the sample's own block is not allocated (bc holds its lookup; a NaN sdf
-        // takes no trilinear read, which would look up other blocks)
-        const bool unallocated = skip && !valid && bc.id < 0;
         if (sdf <= 0.5f && sdf >= -0.5f) sdf = read_sdf_interped<LAYOUT, true>(mv, bc, r.x, r.y, r.z, valid, sdf, valid);
         if (sdf <= 0.0f) break;
         if (sdf >= 0.f && last_sdf < 0.f) return;
         step = valid ? fmaxf(sdf * step_scale, 1.0f) : 2.0f;
-        if (unallocated) step = skip_step(r, dir, bc.bx, bc.by, bc.bz);
         r = make_float3(r.x + dir.x * step, r.y + dir.y * step, r.z + dir.z * step);
         dist_s += step;
     }

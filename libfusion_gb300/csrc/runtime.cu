@@ -70,7 +70,6 @@ gbf_status validate(const gbf_config *c, const gbf_intrinsics *K) {
         return set_error(GBF_ERR_INVALID_ARG, "unknown voxel layout");
     if (c->max_probe < 1) return set_error(GBF_ERR_INVALID_ARG, "max_probe must be >= 1");
     if (c->motion_prior != 0 && c->motion_prior != 1) return set_error(GBF_ERR_INVALID_ARG, "motion_prior must be 0 or 1");
-    if (c->march_skip != 0 && c->march_skip != 1) return set_error(GBF_ERR_INVALID_ARG, "march_skip must be 0 or 1");
     for (int l = 0; l < c->num_levels; ++l)
         if (c->max_iterations[l] < 0 || c->max_iterations[l] > 1000)
             return set_error(GBF_ERR_INVALID_ARG, "max_iterations out of range");
@@ -413,7 +412,6 @@ GBF_API gbf_status gbf_session_create(const gbf_config *cfg, const gbf_intrinsic
     v.pool = cfg->num_blocks;
     v.max_probe = cfg->max_probe;
     v.motion_prior = cfg->motion_prior;
-    v.march_skip = cfg->march_skip;
     v.voxel = cfg->voxel_size;
     v.inv_voxel = 1.0f / cfg->voxel_size;                         // MapState::inverse_voxel_size
     v.tau = cfg->truncation;

@@ -46,7 +46,6 @@ typedef struct or_config {
     float w_icp, w_rgb, icp_dist_thresh, icp_angle_thresh;
     int32_t bilateral;
     int32_t motion_prior;     /* 1: track from the last frame's motion (constant velocity) */
-    int32_t march_skip;       /* 1: jump through an unallocated block in one raycast step */
     int32_t threads;          /* OpenMP threads, 0 = default */
 } or_config;
 

@@ -25,7 +25,7 @@ class OrConfig(C.Structure):
         ("max_iterations", C.c_int32 * MAX_LEVELS),
         ("w_icp", C.c_float), ("w_rgb", C.c_float), ("icp_dist_thresh", C.c_float),
         ("icp_angle_thresh", C.c_float), ("bilateral", C.c_int32), ("motion_prior", C.c_int32),
-        ("march_skip", C.c_int32), ("threads", C.c_int32),
+        ("threads", C.c_int32),
     ]
 
 

@@ -531,26 +531,6 @@ static R read_interp(const MAP *m, R px, R py, R pz, int *valid) {
     return ((R)1 - fz) * r2 + fz * r3;
 }
 
-/* The march's step through an unallocated block when gbf_config::march_skip is
- * set: the reference steps 2 voxels at a time until a sample leaves the block
- * (ray_tracing.cu:399-405); this is the first multiple of 2 past the block's
- * exit, found from the distance t to the nearest exit plane (less 1e-3 voxel,
- * so that rounding can only leave a sample inside the block, from where the
- * next step goes on).  The same operations as the CUDA march. */
-static R skip_step(V3 r, V3 dir, int bx, int by, int bz) {
-    const R inf = (R)INFINITY;
-    const R tx = dir.x > 0 ? ((R)((bx + 1) * 8) - r.x) / dir.x : dir.x < 0 ? ((R)(bx * 8) - r.x) / dir.x : inf;
-    const R ty = dir.y > 0 ? ((R)((by + 1) * 8) - r.y) / dir.y : dir.y < 0 ? ((R)(by * 8) - r.y) / dir.y : inf;
-    const R tz = dir.z > 0 ? ((R)((bz + 1) * 8) - r.z) / dir.z : dir.z < 0 ? ((R)(bz * 8) - r.z) / dir.z : inf;
-    const R t = RFMIN(tx, RFMIN(ty, tz));  /* under 14 voxels (a block's diagonal) */
-    int k = 1;
-    if (t < (R)64) {
-        const int f = (int)RFLOOR((t - (R)1e-3) * (R)0.5) + 1;
-        if (f > 1) k = f;
-    }
-    return (R)(2 * k);
-}
-
 /* MapRenderingDelegate::operator() (ray_tracing.cu:346-425) */
 /* read_colour (ray_tracing.cu:427-441): the colour of the voxel ToVector3i(pt),
  * valid when its weight is not 0 */
@@ -602,10 +582,6 @@ static void ray_pixel(const MAP *m, const M34 *Twc, const M34 *Tcw, int x, int y
         if (sdf >= 0 && last_sdf < 0) return;
         step = valid ? RFMAX(sdf * m->step_scale, (R)1) : (R)2;
         if (g_rs && !valid) g_rs->empty++;
-        if (!valid && m->cfg.march_skip) {
-            const int bx = vtob(floor_r(r.x)), by = vtob(floor_r(r.y)), bz = vtob(floor_r(r.z));
-            if (map_find(m, bx, by, bz) < 0) step = skip_step(r, dir, bx, by, bz);
-        }
         r = v3(r.x + dir.x * step, r.y + dir.y * step, r.z + dir.z * step);
         dist_s += step;
     }

@@ -427,49 +427,3 @@ def test_post_raycast_pyramid_bit_exact(gbf):
         for kind in (0, 1):
             g = s.get_image(1, kind, lvl).cpu().numpy()
             assert np.array_equal(g, of.get(kind, lvl), equal_nan=True), (lvl, kind)
-
-
-@pytest.mark.parametrize("layout", [0, 2])
-def test_raycast_skip_bit_exact_and_close_to_the_reference_march(gbf, layout):
-    """march_skip = 1: a ray crosses a block that is not allocated in one step,
-    to the first 2-voxel step past it, where the reference takes those steps
-    one at a time (ray_tracing.cu:399-405).  The CUDA march and the oracle's,
-    both with the skip, are bit-exact; against the reference march the samples
-    are the same up to the rounding of the accumulated position, so the hit
-    masks agree and the vertices stay within a micrometre (5 mm voxels, the
-    large room, a pose the map was fused from and one aside)."""
-    L = gbf
-    import torch
-    K = H.intrinsics(L, 640, 480)
-    scene = dict(trajectory=1, room=(8, 8, 3), n_spheres=20, n_boxes=12, radius=2.5, speed=0.5, fps=30, seed=2)
-    base = dict(voxel_size=0.005, truncation=0.02, num_buckets=1 << 20, num_blocks=1 << 18)
-    ms, oms = {}, {}
-    fr = H.frames(L, K, 3, step=10, **scene)
-    for skip in (0, 1):
-        cfg = H.small_config(L, layout, march_skip=skip, **base)
-        ms[skip], oms[skip] = L.DenseMapping(K, cfg), _oracle_map(L, cfg, K)
-        for d, c, T in fr:
-            dm = H.depth_m(d)
-            ms[skip].update(H.cuda(dm), H.cuda(c), T)
-            oms[skip].fuse(dm, c, T)
-    T1 = fr[-1][2].copy()
-    T2 = T1.copy()
-    T2[:3, 3] += T1[:3, :3] @ np.array([0.05, -0.03, 0.0])
-    for T in (T1, T2):
-        out = {}
-        for skip in (0, 1):
-            vm = torch.full((K.height, K.width, 4), float("nan"), device="cuda")
-            ms[skip].raycast(vm, T)
-            out[skip] = vm.cpu().numpy()
-        o = oms[1].raycast(T)
-        gh, oh = ~np.isnan(out[1][..., 2]), ~np.isnan(o[..., 2])
-        assert np.array_equal(gh, oh) and gh.mean() > 0.5
-        assert np.array_equal(out[1][gh], o[oh]), "skip march differs from the oracle's"
-        rh = ~np.isnan(out[0][..., 2])
-        both = gh & rh
-        assert np.sum(gh != rh) <= 1e-4 * gh.size, np.sum(gh != rh)
-        dz = np.abs(out[1][both] - out[0][both])
-        print(f"skip vs reference march: hit masks differ {np.sum(gh != rh)}, vertices differing "
-              f"{np.mean(np.any(dz > 0, axis=-1)):.4f}, max {dz.max() * 1e6:.3f} um, "
-              f"p99.9 {np.quantile(dz.max(axis=-1), 0.999) * 1e6:.3f} um")
-        assert np.quantile(dz.max(axis=-1), 0.999) < 1e-6
