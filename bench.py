@@ -244,15 +244,15 @@ class ClockSampler:
 
 
 # DRAM bytes one pixel-iteration of the ICP + photometric reduction moves, from
-# one ncu capture of a level-0 launch over 4 sessions (100.83 MB for 1,228,800
+# one ncu capture of a level-0 launch over 4 sessions (105.50 MB for 1,228,800
 # pixel-iterations, dram__bytes_read.sum + dram__bytes_write.sum): the roofline's traffic
-REDUCE_DRAM_BYTES_PER_PIXEL_ITER = 100.36224e6 / 1228800
-# DRAM bytes per raycast pixel, from one ncu capture of the HALF raycast over 4
-# sessions (66.30 MB read + 4.26 MB written for 4 x 307,200 pixels;
-# same counters), and its issue-active fraction there.
-# The bytes depend on the maps the rays cross, so scaling by pixels is an estimate.
-RAYCAST_DRAM_BYTES_PER_PIXEL = (66.297856e6 + 4.257280e6) / (4 * 307200)
-RAYCAST_ISSUE_ACTIVE = 0.761
+REDUCE_DRAM_BYTES_PER_PIXEL_ITER = (102.155264e6 + 3.340544e6) / 1228800
+# DRAM bytes per raycast pixel, from one ncu capture of the SNORM raycast over 4
+# sessions (66.26 MB read + 4.59 MB written for 4 x 307,200 pixels; same
+# counters), and its issue-active fraction there.  The bytes depend on the maps
+# the rays cross, so scaling by pixels is an estimate.
+RAYCAST_DRAM_BYTES_PER_PIXEL = (66.264576e6 + 4.589312e6) / (4 * 307200)
+RAYCAST_ISSUE_ACTIVE = 0.759
 
 
 def measured_peaks():
@@ -727,13 +727,13 @@ def run_ours(args):
                 "launches_per_step": n_launch, "peak_source": f"{peak_kind} hbm_gbs",
                 "algorithmic_bytes_per_launch": bytes_step / n_launch, "algorithmic_bytes_per_step": bytes_step,
                 "traffic_basis": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0 launch at 4 "
-                                 "sessions: 81.7 B per pixel-iteration, "
+                                 "sessions: 85.9 B per pixel-iteration, "
                                  "times this run's pixel-iterations per launch" if traffic is not None else None,
                 "work_per_step": {"pixel_iterations": pix_iter, "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
                 "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream",
-                "why_this_kernel": "the raycast (37% of launch time against the reduction's 35% in an ncu "
+                "why_this_kernel": "the raycast (38% of launch time against the reduction's 33% in an ncu "
                                    "launch list of the 64-session tick) is bound by instruction issue, not HBM "
-                                   "(76% issue active, DRAM 2.7% in its ncu capture at 4 sessions), so its "
+                                   "(76% issue active, DRAM 2.6% in its ncu capture at 4 sessions), so its "
                                    "figures are under 'march'; the HBM roofline is given for the memory-bound phase",
                 "march_ms_per_step": phases["march"]}
     px_step = sum(s.K.width * s.K.height for s in sessions)
@@ -887,6 +887,14 @@ MIXED_SIZES = ((320, 240), (640, 480), (1280, 720))
 MIXED_VOXELS = (0.004, 0.008, 0.016)
 
 
+def mixed_room(i):
+    """Session i's synthetic room, from 3x3x2.5 m to 10x10x3 m (a golden-ratio
+    sequence over the sessions), the camera circling at 3/8 of the side."""
+    u = (i * 0.6180339887) % 1.0
+    side = 3.0 + 7.0 * u
+    return dict(seed=1000 + i, room=(side, side, 2.5 + 0.5 * u), radius=min(max(0.375 * side, 1.1), 3.5))
+
+
 def mixed_session(L, i):
     """(intrinsics, config) of session i of the mixed workload."""
     w, h = MIXED_SIZES[i % len(MIXED_SIZES)]
@@ -914,7 +922,7 @@ def run_mixed(args):
     nfr = max(warm + steps, n_tune)
     frames, poses0 = [], []
     for i, (K, _) in enumerate(spec):
-        sc = L.SynthScene(seed=1000 + i)
+        sc = L.SynthScene(**mixed_room(i))
         d = torch.empty((nfr, K.height, K.width), dtype=torch.uint16, device="cuda")
         c = torch.empty((nfr, K.height, K.width, 3), dtype=torch.uint8, device="cuda")
         for k in range(nfr):
@@ -982,7 +990,8 @@ def run_mixed(args):
         "metric": METRIC, "workload": "mixed", "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps,
         "warmup": warm, "ms_per_step": total_ms / steps, "higher_is_better": True,
         "config": {"workload": f"{S} sessions per tick: resolutions {['%dx%d' % s for s in MIXED_SIZES]} and voxels "
-                               f"{[f'{v * 1000:.0f} mm' for v in MIXED_VOXELS]} cycled over the sessions",
+                               f"{[f'{v * 1000:.0f} mm' for v in MIXED_VOXELS]} cycled over the sessions, "
+                               f"rooms from 3x3x2.5 to 10x10x3 m",
                    "voxel_layout": LAYOUTS[LAYOUT][1], "launch_shape": shape},
         "latency_ms": {"p50": p(0.5), "p99": p(0.99)}, "clocks": clocks.summary(),
         "plain": {"value": plain, "unit": UNIT, "frames": S * per}, "served_vs_plain": value / plain,
