@@ -1050,7 +1050,7 @@ def run_scale(args):
     torch.cuda.set_stream(stream)
     bufs = [(torch.empty((H, W), dtype=torch.uint16, device="cuda"),
              torch.empty((H, W, 3), dtype=torch.uint8, device="cuda")) for _ in range(2)]
-    max_tris = 1 << 25  # 1.2 GB of vertices: the 2000-frame map meshes to over 2^24 triangles
+    max_tris = 1 << 26  # 2.4 GB of vertices: the 2000-frame map meshes to over 2^25 triangles
     vtx = torch.empty((max_tris, 3, 3), dtype=torch.float32, device="cuda")
     truth = [sc.pose(k) for k in range(n)]
 

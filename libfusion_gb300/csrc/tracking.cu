@@ -402,14 +402,12 @@ struct ReduceSmem {
 // its own 64-thread barrier (staging the whole tile behind the CTA-wide barrier
 // measured 1.4% slower over the track phase).  Warp
 // shuffle tree, then a fixed-order pass over the four warps of each half.
-// Writes 58 floats to part.
-template <bool PACKED>
-__device__ __forceinline__ void cta_partial(ReduceSmem &sm, const SessionView &sv, int level, int rs, int cs,
-                                            const M34 &T, float stddev, int cta, int tile, float *part) {
-    auto &warp_sums = sm.warp_sums;
+// Writes 58 floats to part.  The caller issues the tile's copies first
+// (stage_ref_tile), so that they are in flight while it loads the pose.
+__device__ __forceinline__ void stage_ref_tile(ReduceSmem &sm, const SessionView &sv, int level, int rs, int cta,
+                                               int tile) {
     float4 *s_v = sm.s_v, *s_n = sm.s_n;
     float *s_i = sm.s_i;
-    const PhotoConst pc = photo_const(stddev);
     const int P = sv.lv[level].w * sv.lv[level].h;
     const int first = cta * tile;  // tile <= kCtaPixels, a multiple of 4 (16-byte aligned copies)
     const int n = min(tile, P - first);
@@ -443,7 +441,24 @@ __device__ __forceinline__ void cta_partial(ReduceSmem &sm, const SessionView &s
                 }
             }
         }
-        asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
+}
+
+template <bool PACKED>
+__device__ __forceinline__ void cta_partial(ReduceSmem &sm, const SessionView &sv, int level, int rs, int cs,
+                                            const M34 &T, float stddev, int cta, int tile, float *part) {
+    auto &warp_sums = sm.warp_sums;
+    float4 *s_v = sm.s_v, *s_n = sm.s_n;
+    float *s_i = sm.s_i;
+    const PhotoConst pc = photo_const(stddev);
+    const int P = sv.lv[level].w * sv.lv[level].h;
+    const int first = cta * tile;
+    const int n = min(tile, P - first);
+    {
+        // the pair's own copies done, then its 64-thread barrier
+        const int pair = (threadIdx.x >> 5) & 3;
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
         asm volatile("bar.sync %0, 64;" ::"r"(pair + 1) : "memory");
     }
     const int half = threadIdx.x / kHalfThreads, t = threadIdx.x % kHalfThreads;
@@ -558,6 +573,10 @@ __global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const Sess
     const int level = a.level;
     if (!session_runs(sv, a) || blockIdx.x >= sv.red_ctas[level]) return;
     TrackState *ts = sv.ts;
+    const int rs = ts->idx, cs = 1 - rs;
+    // the reference tile's copies first: in flight while the pose is loaded
+    __shared__ ReduceSmem sm;
+    stage_ref_tile(sm, sv, level, rs, blockIdx.x, sv.red_tile[level]);
     __shared__ M34 T;
     __shared__ float stddev_s;
     if (threadIdx.x == 0) {
@@ -571,8 +590,6 @@ __global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const Sess
         }
     }
     __syncthreads();
-    const int rs = ts->idx, cs = 1 - ts->idx;
-    __shared__ ReduceSmem sm;
     cta_partial<true>(sm, sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.red_tile[level],
                 sv.partials + (size_t)blockIdx.x * kPartialStride);
     __threadfence();
@@ -846,12 +863,13 @@ static __device__ __align__(256) float g_reduce_scratch[kStaticTicketSlot + 64];
 __global__ void __launch_bounds__(kReduceThreads, 3) reduce_static_kernel(SessionView sv, ReduceArgs a,
                                                                           float *scratch, double *out) {
     const int nctas = sv.red_ctas[0];
+    __shared__ ReduceSmem sm;
+    stage_ref_tile(sm, sv, 0, 0, blockIdx.x, kCtaPixels);
     __shared__ M34 T;
     if (threadIdx.x == 0)
 #pragma unroll
         for (int i = 0; i < 12; ++i) T.m[i] = a.pose[i];
     __syncthreads();
-    __shared__ ReduceSmem sm;
     cta_partial<false>(sm, sv, 0, 0, 1, T, a.stddev, blockIdx.x, kCtaPixels, scratch + (size_t)blockIdx.x * kPartialStride);
     __threadfence();
     __syncthreads();
