@@ -561,6 +561,7 @@ def serve_run(L, K, seconds: float, groups: int, stream, rate: float = 4.0, slot
         srv.submit(r)
     srv.run(seconds)
     rep = srv.report()
+    rep["graphs_captured"] = batch.captures()  # 2 (one per tick parity): admissions never re-capture
     for slot, x in enumerate(srv.live):
         if x is not None:
             batch.set(slot, None)

@@ -458,6 +458,10 @@ GBF_API gbf_status gbf_batch_set_timing(gbf_batch *b, int32_t enable);
 GBF_API gbf_status gbf_batch_phase_ms(gbf_batch *b, float *ms, int32_t n);
 /* Number of kernel launches one tick makes. */
 GBF_API gbf_status gbf_batch_kernels(gbf_batch *b, int32_t *n);
+/* Tick graphs the batch has captured so far (one per tick parity for each tick
+ * shape; a change of shape, groups, stagger, tile or timing drops them).  A
+ * server watches it to see that admissions and evictions do not re-capture. */
+GBF_API gbf_status gbf_batch_captures(gbf_batch *b, int64_t *n);
 
 /* ---- synthetic RGB-D scenes (test and benchmark input) ------------------------ */
 typedef struct gbf_synth_params {

@@ -416,6 +416,12 @@ class FusionBatch:
         d["ticks"] = int(out[7])
         return d
 
+    def captures(self) -> int:
+        """Tick graphs captured so far."""
+        n = C.c_int64()
+        call("gbf_batch_captures", self._h, C.byref(n))
+        return int(n.value)
+
     def kernels_per_tick(self) -> int:
         n = C.c_int32()
         call("gbf_batch_kernels", self._h, C.byref(n))

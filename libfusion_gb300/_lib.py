@@ -158,6 +158,7 @@ SIGNATURES = {
     "gbf_batch_results": (C.c_int, [_P, _I32, _P, _I32]),
     "gbf_batch_phase_ms": (C.c_int, [_P, C.POINTER(C.c_float), _I32]),
     "gbf_batch_kernels": (C.c_int, [_P, C.POINTER(_I32)]),
+    "gbf_batch_captures": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "gbf_synth_default": (C.c_int, [C.POINTER(SynthParams)]),
     "gbf_synth_create": (C.c_int, [C.POINTER(SynthParams), C.POINTER(_P)]),
     "gbf_synth_destroy": (C.c_int, [_P]),

@@ -114,4 +114,5 @@ struct gbf_batch {
     gbf::Extent floor_ex{};
     int floor_slots = 0;
     int floor_layouts[gbf::kNumLayouts] = {};
+    long long captures = 0;             // tick graphs captured (gbf_batch_captures)
 };

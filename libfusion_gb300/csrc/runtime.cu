@@ -1038,7 +1038,7 @@ static void batch_reshape(gbf_batch *b) {
     for (int i = 0; i < b->max_slots; ++i) {
         gbf_session *t = b->sessions[i];
         if (!t) continue;
-        nslots = i + 1;
+        nslots = std::max(nslots, i + 1);
         ex.w = std::max(ex.w, t->ex.w);
         ex.h = std::max(ex.h, t->ex.h);
         ex.max_pool = std::max(ex.max_pool, t->ex.max_pool);
@@ -1419,6 +1419,7 @@ GBF_API gbf_status gbf_batch_process(gbf_batch *b, const uint8_t *active, int32_
             e = cudaGraphInstantiate(&b->exec[k], g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return cuda_error(e, "gbf_batch_process: instantiate");
+            b->captures += 1;
         }
         cudaError_t e = cudaGraphLaunch(b->exec[k], st);
         if (e != cudaSuccess) return cuda_error(e, "gbf_batch_process: launch");
@@ -1646,6 +1647,13 @@ GBF_API gbf_status gbf_batch_phase_ms(gbf_batch *b, float *ms, int32_t n) {
         }
     for (int i = 0; i < kPhases; ++i) ms[i] = b->phase_n ? (float)(b->phase_sum[i] / b->phase_n) : 0.f;
     if (n > kPhases) ms[kPhases] = (float)b->phase_n;
+    return GBF_OK;
+}
+
+GBF_API gbf_status gbf_batch_captures(gbf_batch *b, int64_t *n) {
+    if (!b || !n) return set_error(GBF_ERR_INVALID_ARG, "gbf_batch_captures: null");
+    std::lock_guard<std::mutex> lock(b->mu);
+    *n = b->captures;
     return GBF_OK;
 }
 

@@ -246,6 +246,79 @@ def test_batch_churn_keeps_graph_and_results(gbf):
     b.close()
 
 
+def test_reserved_batch_admits_smaller_sessions_without_recapture(gbf):
+    """A batch reserved for three slots of the largest configuration it serves
+    admits and evicts sessions of a smaller block pool, and leaves a slot empty,
+    without capturing its tick again: two graphs (one per tick parity) for the
+    whole run.  Every session's poses and map equal the same frames processed
+    alone.  The same churn in a batch with no reservation re-captures."""
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    big = H.small_config(L, 1)
+    small = H.small_config(L, 1, num_blocks=1 << 14, num_buckets=1 << 16)
+    fr = [H.frames(L, K, 6, seed=70 + i) for i in range(4)]
+    # (slot, config, sequence, first tick, last tick + 1)
+    plan = [(0, small, 0, 0, 6), (1, big, 1, 0, 3), (2, small, 2, 2, 6), (1, small, 3, 3, 6)]
+
+    def alone(cfg, f, frames):
+        s = L.System(K, cfg)
+        s.set_pose(f[frames[0]][2])
+        for k in frames:
+            s.process_images(H.cuda(f[k][0]), H.cuda(f[k][1]))
+        torch.cuda.synchronize()
+        return s.get_camera_pose(), s.export()
+
+    def run(reserve):
+        b = L.FusionBatch(3)
+        if reserve:
+            b.reserve(K, big, 3)
+        slots, done = [None] * 3, []
+        for k in range(6):
+            for j, (slot, cfg, seq, k0, k1) in enumerate(plan):
+                if k == k1 and slots[slot] is not None and slots[slot][0] == j:
+                    b.flush()
+                    torch.cuda.synchronize()
+                    done.append((j, slots[slot][1].get_camera_pose(), slots[slot][1].export()))
+                    b.set(slot, None)
+                    slots[slot] = None
+            for j, (slot, cfg, seq, k0, k1) in enumerate(plan):
+                if k == k0:
+                    s = L.System(K, cfg)
+                    s.set_pose(fr[seq][k][2])
+                    b.set(slot, s)
+                    slots[slot] = (j, s)
+            active = [x is not None for x in slots]
+            for slot, x in enumerate(slots):
+                if x is not None:
+                    f = fr[plan[x[0]][2]][k]
+                    x[1].stage(H.cuda(f[0]), H.cuda(f[1]))
+            b.process(active, use_graph=True)
+            if k == 1:
+                first = b.captures()
+        b.flush()
+        torch.cuda.synchronize()
+        for x in slots:
+            if x is not None:
+                done.append((x[0], x[1].get_camera_pose(), x[1].export()))
+        n = b.captures()
+        b.close()
+        return sorted(done, key=lambda d: d[0]), first, n
+
+    got, first, n = run(True)
+    assert first == 2 and n == 2, (first, n)
+    assert [d[0] for d in got] == list(range(len(plan)))
+    for (j, pose, m), (slot, cfg, seq, k0, k1) in zip(got, plan):
+        want_pose, want_map = alone(cfg, fr[seq], range(k0, k1))
+        assert np.array_equal(pose, want_pose), j
+        for x, y in zip(H.sort_blocks(*m), H.sort_blocks(*want_map)):
+            assert np.array_equal(x, y), j
+    got2, _, n2 = run(False)
+    assert n2 > 2
+    for a, c in zip(got, got2):
+        assert np.array_equal(a[1], c[1])
+
+
 def test_autotune_explores_settles_and_keeps_results(gbf):
     """The online tuner switches groups, stagger and raycast tile while the batch
     serves: every tick's poses and the final maps equal those of a batch with a
