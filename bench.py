@@ -1092,6 +1092,16 @@ def run_scale(args):
     frame_ms = [a.elapsed_time(b) for a, b in frame_ms]
     mesh_ms = [a.elapsed_time(b) for a, b in mesh_ms]
     st = s.stats()
+    # block garbage collection on the full map: the blocks farther than 3 m from
+    # the last camera pruned on the stream (gbf_map_prune_async), timed by events
+    a3, b3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a3.record(stream)
+    s.prune_async(center=poses[-1][:3, 3], radius=3.0, stream=stream)
+    b3.record(stream)
+    torch.cuda.synchronize()
+    collection = {"kind": "gbf_map_prune_async, blocks farther than 3 m from the last camera",
+                  "blocks_before": st.allocated_blocks, "blocks_after": s.stats().allocated_blocks,
+                  "ms": a3.elapsed_time(b3)}
     s.close()
     total_ms = sum(frame_ms) + sum(mesh_ms)
     poses = np.array(poses)
@@ -1162,6 +1172,7 @@ def run_scale(args):
         "phases": phases, "peak_gbs": peak, "peak_source": f"{peak_kind} hbm_gbs",
         "work_per_frame": {k: v / n for k, v in work.items() if k in ("pixel_iterations", "integrated_blocks")},
         "map": {"allocated_blocks": st.allocated_blocks, "status": st.status},
+        "collection": collection,
         "tracking": {"failed_frames": failed, "ate_vs_ground_truth_mm": float(np.sqrt(np.mean(err ** 2)) * 1e3),
                      "max_error_mm": float(err.max() * 1e3)},
         "clocks": clocks.summary(),

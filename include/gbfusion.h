@@ -339,18 +339,29 @@ GBF_API gbf_status gbf_map_read_dump(gbf_session *s, const char *path);
 
 /* ---- block garbage collection ------------------------------------------------- */
 /* deleteBlock (src/data_struct/map_struct.cu:327-363) for a list of blocks: their
- * voxels and table entries go, the pool is compacted.  The reference defines
+ * voxels and table entries go, the pool is compacted (the kept blocks above the
+ * new pool end move into the freed positions below it) and the table is
+ * rebuilt from the kept blocks, all on the device.  The reference defines
  * deleteBlock but never calls it (its one caller is commented out,
  * depth_fusion.cu:70), so its pool only grows; a long-running session prunes
  * here.  A deleted block that is observed again starts from zero, as a block
- * the reference re-creates would.  Pose and tracking state are kept.
- * Synchronises; *n_deleted (may be NULL) = blocks removed. */
+ * the reference re-creates would.  Pose and tracking state are kept; the last
+ * fuse's visible list is emptied (its block ids no longer hold).  Blocks not
+ * in the map are ignored.  Synchronises; *n_deleted (may be NULL) = blocks
+ * removed. */
 GBF_API gbf_status gbf_map_delete_blocks(gbf_session *s, const int32_t *coords, int64_t n, int64_t *n_deleted);
 /* Delete the blocks whose centre lies farther than `radius` metres from
  * `center` (world frame; center NULL or radius < 0: no distance test) and, with
- * drop_unobserved, the blocks without any observed voxel (all weights 0). */
+ * drop_unobserved, the blocks without any observed voxel (all weights 0).
+ * Synchronises; *n_deleted (may be NULL) = blocks removed. */
 GBF_API gbf_status gbf_map_prune(gbf_session *s, const double center[3], double radius, int32_t drop_unobserved,
                                  int64_t *n_deleted);
+/* gbf_map_prune enqueued on `stream` with no host synchronisation and no
+ * allocation, for a serving loop that collects between frames: a handful of
+ * launches in the session's stream order (after its last frame's fusion, before
+ * its next).  The count is not returned; gbf_get_stats gives the blocks left. */
+GBF_API gbf_status gbf_map_prune_async(gbf_session *s, const double center[3], double radius,
+                                       int32_t drop_unobserved, void *stream);
 
 /* Visible-block list of the last fuse (block coordinates), synchronises. */
 GBF_API gbf_status gbf_visible_blocks(gbf_session *s, int32_t *coords, int64_t max_blocks, int64_t *n_blocks);

@@ -249,6 +249,12 @@ class DenseMapping(_Session):
         call("gbf_map_prune", self._h, ctr, float(radius), 1 if drop_unobserved else 0, C.byref(n))
         return int(n.value)
 
+    def prune_async(self, center=None, radius: float = -1.0, drop_unobserved: bool = False, stream=None) -> None:
+        """prune() enqueued on `stream` (default: torch's current stream) with
+        no host synchronisation; stats().allocated_blocks gives what is left."""
+        ctr = None if center is None else (C.c_double * 3)(*[float(x) for x in center])
+        call("gbf_map_prune_async", self._h, ctr, float(radius), 1 if drop_unobserved else 0, _stream(stream))
+
     def visible_blocks(self) -> np.ndarray:
         n = C.c_int64()
         call("gbf_visible_blocks", self._h, None, 0, C.byref(n))

@@ -54,6 +54,7 @@ enum Counter {
     C_TICKET = 5,     // last-CTA-done ticket of the reduction
     C_MESH_BLOCKS = 6,
     C_MESH_TRIS = 7,
+    C_GC_DELETED = 8, // blocks deleted by the last garbage collection
     C_COUNT = 16
 };
 

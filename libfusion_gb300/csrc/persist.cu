@@ -256,88 +256,4 @@ GBF_API gbf_status gbf_map_read_dump(gbf_session *s, const char *path) {
     return gbf_map_import(s, c.data(), sd.data(), w.data(), rgb.data(), n);
 }
 
-// Keep the blocks whose flag is set: the map is rebuilt from them (reset, then
-// import), so the pool is compacted and the table holds no tombstones.
-static gbf_status rebuild_map(gbf_session *s, const std::vector<int32_t> &c, const std::vector<float> &sd,
-                              const std::vector<float> &w, const std::vector<uint8_t> &rgb,
-                              const std::vector<char> &keep, int64_t *n_deleted) {
-    const int64_t n = (int64_t)keep.size();
-    int64_t kept = 0;
-    for (char k : keep) kept += k ? 1 : 0;
-    if (n_deleted) *n_deleted = n - kept;
-    if (kept == n) return GBF_OK;
-    std::vector<int32_t> c2((size_t)kept * 3);
-    std::vector<float> s2((size_t)kept * kVox), w2((size_t)kept * kVox);
-    std::vector<uint8_t> r2((size_t)kept * kVox * 3);
-    for (int64_t b = 0, o = 0; b < n; ++b) {
-        if (!keep[b]) continue;
-        std::memcpy(&c2[o * 3], &c[b * 3], 3 * sizeof(int32_t));
-        std::memcpy(&s2[o * kVox], &sd[b * kVox], kVox * sizeof(float));
-        std::memcpy(&w2[o * kVox], &w[b * kVox], kVox * sizeof(float));
-        std::memcpy(&r2[o * kVox * 3], &rgb[b * kVox * 3], kVox * 3);
-        ++o;
-    }
-    gbf_status st = reset_map(s);
-    if (st != GBF_OK) return st;
-    return gbf_map_import(s, c2.data(), s2.data(), w2.data(), r2.data(), kept);
-}
-
-static gbf_status export_all(gbf_session *s, std::vector<int32_t> &c, std::vector<float> &sd, std::vector<float> &w,
-                             std::vector<uint8_t> &rgb) {
-    int64_t n = 0;
-    gbf_status st = gbf_map_export(s, nullptr, nullptr, nullptr, nullptr, 0, &n);
-    if (st != GBF_OK) return st;
-    c.assign((size_t)n * 3, 0);
-    sd.assign((size_t)n * kVox, 0.f);
-    w.assign((size_t)n * kVox, 0.f);
-    rgb.assign((size_t)n * kVox * 3, 0);
-    if (n == 0) return GBF_OK;
-    return gbf_map_export(s, c.data(), sd.data(), w.data(), rgb.data(), n, &n);
-}
-
-GBF_API gbf_status gbf_map_delete_blocks(gbf_session *s, const int32_t *coords, int64_t n, int64_t *n_deleted) {
-    if (!s || n < 0 || (n > 0 && !coords)) return set_error(GBF_ERR_INVALID_ARG, "gbf_map_delete_blocks: null");
-    std::set<std::tuple<int, int, int>> gone;
-    for (int64_t i = 0; i < n; ++i) gone.insert(std::make_tuple(coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]));
-    std::vector<int32_t> c;
-    std::vector<float> sd, w;
-    std::vector<uint8_t> rgb;
-    gbf_status st = export_all(s, c, sd, w, rgb);
-    if (st != GBF_OK) return st;
-    const int64_t m = (int64_t)c.size() / 3;
-    std::vector<char> keep((size_t)m, 1);
-    for (int64_t b = 0; b < m; ++b)
-        if (gone.count(std::make_tuple(c[3 * b], c[3 * b + 1], c[3 * b + 2]))) keep[b] = 0;
-    return rebuild_map(s, c, sd, w, rgb, keep, n_deleted);
-}
-
-GBF_API gbf_status gbf_map_prune(gbf_session *s, const double center[3], double radius, int32_t drop_unobserved,
-                                 int64_t *n_deleted) {
-    if (!s) return set_error(GBF_ERR_INVALID_ARG, "gbf_map_prune: null");
-    std::vector<int32_t> c;
-    std::vector<float> sd, w;
-    std::vector<uint8_t> rgb;
-    gbf_status st = export_all(s, c, sd, w, rgb);
-    if (st != GBF_OK) return st;
-    const int64_t m = (int64_t)c.size() / 3;
-    const double bm = 8.0 * (double)s->cfg.voxel_size;  // block edge in metres
-    std::vector<char> keep((size_t)m, 1);
-    for (int64_t b = 0; b < m; ++b) {
-        if (center && radius >= 0.0) {
-            double d2 = 0.0;
-            for (int k = 0; k < 3; ++k) {
-                const double x = ((double)c[3 * b + k] + 0.5) * bm - center[k];  // block centre
-                d2 += x * x;
-            }
-            if (d2 > radius * radius) keep[b] = 0;
-        }
-        if (keep[b] && drop_unobserved) {
-            bool seen = false;
-            for (int i = 0; i < kVox && !seen; ++i) seen = w[(size_t)b * kVox + i] != 0.f;
-            if (!seen) keep[b] = 0;
-        }
-    }
-    return rebuild_map(s, c, sd, w, rgb, keep, n_deleted);
-}
-
 }  // extern "C"

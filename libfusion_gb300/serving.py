@@ -19,6 +19,11 @@ Latency of a frame: from the moment its camera produced it (admission time +
 index / fps) to the moment its pose is on the host.  The wait for admission is
 reported separately, per request.
 
+Block garbage collection (optional): every `collect_every` fused frames of a
+session, `collect(session, pose, stream)` runs between two ticks with the pose
+its last frame tracked -- typically gbf_map_prune_async around the camera,
+stream-ordered with the batch's launches and with no host synchronisation.
+
 The clock, the batch and the session factory are parameters, so the scheduling
 is testable without a GPU.
 """
@@ -134,8 +139,11 @@ class Server:
     may look past a head that does not fit in memory."""
 
     def __init__(self, batch, slots: int, cache: ArenaCache, clock=None, set_pose=None, stream=None,
-                 use_graph: bool = True, look_ahead: int = 8, record_poses: bool = False):
+                 use_graph: bool = True, look_ahead: int = 8, record_poses: bool = False, collect=None,
+                 collect_every: int = 0):
         self.batch, self.slots, self.cache = batch, slots, cache
+        self.collect, self.collect_every = collect, collect_every
+        self.collections = 0
         self.clock = clock or WallClock()
         self.set_pose = set_pose or (lambda s, T: s.set_pose(T))
         self.stream, self.use_graph, self.look_ahead = stream, use_graph, look_ahead
@@ -247,6 +255,9 @@ class Server:
             x.fused += 1
             if x.next_frame >= x.req.frames:
                 self._evict(i)
+            elif self.collect is not None and self.collect_every > 0 and x.fused % self.collect_every == 0:
+                self.collect(x.session, poses[i], self.stream)
+                self.collections += 1
         return True
 
     def run(self, until: float) -> None:
@@ -282,6 +293,7 @@ class Server:
                            "p99": _pct(self.latency_ms, 0.99),
                            "max": max(self.latency_ms) if self.latency_ms else None},
             "tracking_failed_frames": self.failed_frames,
+            "collections": self.collections,
             "memory": {"budget_bytes": self.cache.budget, "peak_bytes": self.cache.peak_bytes,
                        "arenas_created": self.cache.created, "arenas_reused": self.cache.reused,
                        "arenas_freed": self.cache.freed},

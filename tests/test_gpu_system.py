@@ -548,13 +548,17 @@ def test_motion_prior_matches_oracle(gbf):
     assert np.abs(gp[:, :3, 3] - truth[:, :3, 3]).max() < 0.02
 
 
-def test_server_results_alone_and_in_the_mix(gbf):
+@pytest.mark.parametrize("collect", [False, True])
+def test_server_results_alone_and_in_the_mix(gbf, collect):
     """The continuous-batching server (libfusion_gb300/serving.py) on the GPU:
     three requests of two voxel sizes through a two-slot batch whose memory
     budget holds two session arenas.  The third request waits for a slot,
     takes the memory of an evicted session, and every session's poses, frame
     by frame, equal those of the same frames run alone on the plain path, bit
-    for bit, whatever else shared its ticks."""
+    for bit, whatever else shared its ticks.  With collection, every third
+    fused frame of a session prunes its map around the tracked camera between
+    ticks (gbf_map_prune_async on the server's stream); the plain path prunes
+    synchronously after the same frames."""
     import torch
     from libfusion_gb300.serving import ArenaCache, Request, Server
     L = gbf
@@ -578,7 +582,12 @@ def test_server_results_alone_and_in_the_mix(gbf):
     batch.set_groups(1)
     cache = ArenaCache(nbytes[8] + nbytes[10], make=lambda key: L.System(K, cfgs[key[0]]),
                        destroy=lambda s: s.close(), reset=lambda s: s.reset())
-    srv = Server(batch, 2, cache, record_poses=True)
+    every, radius = 3, 1.2
+
+    def prune(s, pose, stream):
+        s.prune_async(center=np.asarray(pose)[:3, 3], radius=radius, drop_unobserved=True, stream=stream)
+
+    srv = Server(batch, 2, cache, record_poses=True, collect=prune if collect else None, collect_every=every)
     for sid, t, v, n, _ in spec:
         d, c, T0 = frames[sid]
         srv.submit(Request(sid=sid, arrival=t, frames=n, key=(v,), nbytes=nbytes[v], pose0=T0, fps=200.0,
@@ -589,13 +598,72 @@ def test_server_results_alone_and_in_the_mix(gbf):
     assert rep["deferred_by_slots"] >= 1 and rep["concurrency_peak"] == 2
     assert rep["memory"]["peak_bytes"] <= nbytes[8] + nbytes[10]
     assert rep["tracking_failed_frames"] == 0
+    assert rep["collections"] == (sum((n - 1) // every for _, _, _, n, _ in spec) if collect else 0)
     batch.close()
     cache.close()
+    pruned = 0
     for sid, _, v, n, _ in spec:
         d, c, T0 = frames[sid]
         s = L.System(K, cfgs[v])
         s.set_pose(T0)
         for k in range(n):
             s.process_images(d[k], c[k])
-            assert np.array_equal(s.get_camera_pose(), srv.poses[(sid, k)]), (sid, k)
+            pose = s.get_camera_pose()
+            assert np.array_equal(pose, srv.poses[(sid, k)]), (sid, k)
+            if collect and (k + 1) % every == 0 and k + 1 < n:
+                pruned += s.prune(center=pose[:3, 3], radius=radius, drop_unobserved=True)
         s.close()
+    assert pruned > 0 or not collect
+
+
+def test_prune_between_graph_ticks_matches_session_alone(gbf):
+    """Serving loop garbage collection: one session of a two-slot batch prunes
+    its map (radius around its camera, and unobserved blocks) on the batch's
+    stream between two graph ticks, with no host synchronisation.  Its poses and
+    map equal the same frames processed alone with a synchronous prune at the
+    same frame; the other session is undisturbed."""
+    import torch
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 2)
+    n_fr, at = 6, 3
+    fr = [H.frames(L, K, n_fr, seed=90 + i) for i in range(2)]
+    radius = 1.2
+
+    def alone(i, prune):
+        s = L.System(K, cfg)
+        s.set_pose(fr[i][0][2])
+        for k, (d, c, T) in enumerate(fr[i]):
+            if prune and k == at:
+                n = s.prune(center=s.get_camera_pose()[:3, 3], radius=radius, drop_unobserved=True)
+                assert n > 0
+            s.process_images(H.cuda(d), H.cuda(c))
+        torch.cuda.synchronize()
+        return s.get_camera_pose(), s.export()
+
+    ss = [L.System(K, cfg) for _ in range(2)]
+    for s, f in zip(ss, fr):
+        s.set_pose(f[0][2])
+    b = L.FusionBatch(2)
+    for i, s in enumerate(ss):
+        b.set(i, s)
+    stream = torch.cuda.current_stream()
+    for k in range(n_fr):
+        if k == at:
+            b.flush()
+            torch.cuda.synchronize()
+            cam = ss[0].get_camera_pose()[:3, 3]
+            n_before = ss[0].stats().allocated_blocks
+            ss[0].prune_async(center=cam, radius=radius, drop_unobserved=True, stream=stream)
+        for i, s in enumerate(ss):
+            s.stage(H.cuda(fr[i][k][0]), H.cuda(fr[i][k][1]))
+        b.process([True, True], use_graph=True, stream=stream)
+    b.flush()
+    torch.cuda.synchronize()
+    for i, s in enumerate(ss):
+        pose, m = alone(i, prune=(i == 0))
+        assert np.array_equal(s.get_camera_pose(), pose), i
+        for x, y in zip(H.sort_blocks(*s.export()), H.sort_blocks(*m)):
+            assert np.array_equal(x, y), i
+    b.close()
+    assert n_before > 0

@@ -320,3 +320,38 @@ def test_delete_and_prune_blocks(gbf):
     assert m.prune(drop_unobserved=True) >= 1
     after = {tuple(x) for x in m.export()[0]}
     assert (9999, 9999, 9999) not in after and len(after) <= n_before - 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("layout", [0, 1, 2])
+def test_collection_of_half_the_blocks_keeps_the_rest_reachable(gbf, layout):
+    """A random half of the blocks deleted: many kept blocks sit above the new
+    pool end and move into freed positions below it.  The kept blocks keep
+    their voxels bit for bit, the pool shrinks to them, the rebuilt table finds
+    every kept block (deleting them by list finds them all), and fusing on
+    equals fusing on from a fresh map holding the kept blocks."""
+    import torch
+    L = gbf
+    K, m, T = _fused(L, layout, n=4)
+    c0, s0, w0, r0 = m.export()
+    n0 = len(c0)
+    rng = np.random.default_rng(7)
+    keep = rng.random(n0) < 0.5
+    assert m.delete_blocks(c0[~keep]) == int((~keep).sum())
+    assert m.stats().allocated_blocks == int(keep.sum())
+    c1, s1, w1, r1 = m.export()
+    for x, y in zip(H.sort_blocks(c0[keep], s0[keep], w0[keep], r0[keep]), H.sort_blocks(c1, s1, w1, r1)):
+        np.testing.assert_array_equal(x, y)
+    fresh = L.DenseMapping(K, H.small_config(L, layout))
+    fresh.import_blocks(c1, s1, w1, r1)
+    d, c, T2 = H.frames(L, K, 1, start=14)[0]
+    for mm in (m, fresh):
+        mm.update(H.cuda(H.depth_m(d)), H.cuda(c), T2)
+    torch.cuda.synchronize()
+    a = H.sort_blocks(*m.export())
+    b = H.sort_blocks(*fresh.export())
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    # every block of the map is found in the rebuilt table
+    c2 = m.export()[0]
+    assert m.delete_blocks(c2) == len(c2) and m.stats().allocated_blocks == 0

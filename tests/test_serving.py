@@ -40,7 +40,12 @@ class FakeBatch:
         self.clock.t += self.base + self.per_frame * n
 
     def results(self, back=0):
-        return None, [1] * len(self.slots), None, None
+        # each slot's "pose": a translation by (slot, ticks so far)
+        poses = []
+        for i in range(len(self.slots)):
+            T = [[1.0, 0, 0, float(i)], [0, 1.0, 0, float(len(self.ticks))], [0, 0, 1.0, 0], [0, 0, 0, 1.0]]
+            poses.append(T)
+        return poses, [1] * len(self.slots), None, None
 
 
 class Arena:
@@ -168,3 +173,24 @@ def test_arrivals_count_from_the_server_start():
     srv.run(6.0)
     r = srv.report()
     assert r["admitted"] == 2 and r["queue_wait_s"]["max"] < 0.1
+
+
+def test_collection_runs_every_n_frames_between_ticks_with_the_tracked_pose():
+    clock = FakeClock()
+    batch = FakeBatch(clock, 2)
+    calls = []
+
+    def collect(session, pose, stream):
+        calls.append((session.id, len(batch.ticks), pose[0][3], pose[1][3], stream))
+
+    srv = Server(batch, 2, make_cache(100), clock=clock, set_pose=lambda s, T: None, stream="st",
+                 collect=collect, collect_every=4)
+    srv.submit(req(0, 0.0, frames=10))
+    srv.run(2.0)
+    r = srv.report()
+    assert r["frames"] == 10 and r["completed"] == 1
+    # after its 4th and 8th frames (not after the last: the session leaves), with
+    # the pose of the tick that fused that frame, on the server's stream
+    assert r["collections"] == 2
+    assert [c[1] for c in calls] == [4, 8]
+    assert [c[3] for c in calls] == [4.0, 8.0] and all(c[2] == 0.0 and c[4] == "st" for c in calls)
