@@ -465,14 +465,28 @@ __device__ __forceinline__ void cta_partial(ReduceSmem &sm, const SessionView &s
     float acc[29];
 #pragma unroll
     for (int k = 0; k < 29; ++k) acc[k] = 0.f;
+    if (n == kCtaPixels) {
+        // a full tile (every CTA but a level's last): a fixed trip count with no
+        // bound test lets the compiler overlap one pixel's gathers with the
+        // previous pixel's rows (track phase 3.92 -> 3.72 ms against the loop below)
 #pragma unroll 2
-    for (int i = 0; i < kCtaPixels / kHalfThreads; ++i) {
-        const int c = t + i * kHalfThreads;
-        if (c >= n) break;
-        float row[7];
-        const bool ok = half == 0 ? icp_row(sv, level, cs, T, s_v[c], s_n[c], row)
-                                  : rgb_row<PACKED>(sv, level, cs, T, pc, s_v[c], s_i[c], row);
-        if (ok) accumulate(acc, row);
+        for (int i = 0; i < kCtaPixels / kHalfThreads; ++i) {
+            const int c = t + i * kHalfThreads;
+            float row[7];
+            const bool ok = half == 0 ? icp_row(sv, level, cs, T, s_v[c], s_n[c], row)
+                                      : rgb_row<PACKED>(sv, level, cs, T, pc, s_v[c], s_i[c], row);
+            if (ok) accumulate(acc, row);
+        }
+    } else {
+#pragma unroll 2
+        for (int i = 0; i < kCtaPixels / kHalfThreads; ++i) {
+            const int c = t + i * kHalfThreads;
+            if (c >= n) break;
+            float row[7];
+            const bool ok = half == 0 ? icp_row(sv, level, cs, T, s_v[c], s_n[c], row)
+                                      : rgb_row<PACKED>(sv, level, cs, T, pc, s_v[c], s_i[c], row);
+            if (ok) accumulate(acc, row);
+        }
     }
     const float total = warp_sum29(acc);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
