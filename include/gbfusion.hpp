@@ -127,6 +127,26 @@ class DenseMapping : public Session {
               "DenseMapping::raycast");
     }
     void reset_mapping(void *stream = nullptr) { check(gbf_session_reset(handle(), stream), "reset_mapping"); }
+    // deleteBlock (map_struct.cu:327-363) for the listed block coordinates (x, y, z per
+    // block); returns the blocks removed
+    int64_t delete_blocks(const std::vector<int32_t> &coords) {
+        int64_t n = 0;
+        check(gbf_map_delete_blocks(handle(), coords.empty() ? nullptr : coords.data(), (int64_t)(coords.size() / 3),
+                                    &n), "DenseMapping::delete_blocks");
+        return n;
+    }
+    // the blocks farther than radius from center (nullptr: no distance test) and,
+    // with drop_unobserved, those without an observed voxel; returns the blocks removed
+    int64_t prune(const double *center, double radius, bool drop_unobserved = false) {
+        int64_t n = 0;
+        check(gbf_map_prune(handle(), center, radius, drop_unobserved ? 1 : 0, &n), "DenseMapping::prune");
+        return n;
+    }
+    // prune() on `stream`, no host synchronisation (between the ticks of a batch)
+    void prune_async(const double *center, double radius, bool drop_unobserved = false, void *stream = nullptr) {
+        check(gbf_map_prune_async(handle(), center, radius, drop_unobserved ? 1 : 0, stream),
+              "DenseMapping::prune_async");
+    }
     // mesh buffers are caller-allocated device memory of max_tris triangles (system.h:36-41)
     size_t fetch_mesh_vertex_only(void *vertex, size_t max_tris) {
         uint64_t n = 0;
@@ -218,6 +238,12 @@ class FusionBatch {
     // to that size then come and go without a new captured graph
     void reserve(const gbf_config &cfg, const gbf_intrinsics &K, int slots) {
         check(gbf_batch_reserve(handle(), &cfg, &K, slots), "FusionBatch::reserve");
+    }
+    // tick graphs captured so far
+    int64_t captures() {
+        int64_t n = 0;
+        check(gbf_batch_captures(handle(), &n), "FusionBatch::captures");
+        return n;
     }
     // frames read from device memory at each tick (nullptr, nullptr: the session's staging)
     void set_inputs(int slot, const uint16_t *depth_dev, const uint8_t *rgb_dev) {

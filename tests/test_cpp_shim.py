@@ -51,7 +51,9 @@ BATCH_SRC = r'''
 #include <cstdio>
 #include <cstring>
 // Two sessions served by a tuned FusionBatch against a third processing the
-// same frames alone through System::process_images: bit-identical poses.
+// same frames alone through System::process_images: bit-identical poses.  Half
+// way, the batched sessions prune their maps between ticks (prune_async) and the
+// lone one synchronously, around the same camera.
 int main() {
     fusion::IntrinsicMatrix K(320, 240, 262.5f, 262.5f, 159.75f, 119.75f);
     gbf_config c = fusion::default_config();
@@ -82,9 +84,18 @@ int main() {
     batch.set(0, &a);
     batch.set(1, &b);
     batch.autotune(true, 2);
+    long long pruned = 0;
     for (int f = 0; f < n; ++f) {
         uint16_t *d = depth + (size_t)f * W * H;
         uint8_t *r = rgb + (size_t)f * W * H * 3;
+        if (f == n / 2) {
+            batch.flush();
+            const fusion::Pose p = alone.get_camera_pose();
+            const double cam[3] = {p.data()[3], p.data()[7], p.data()[11]};
+            a.prune_async(cam, 1.0, true);
+            b.prune_async(cam, 1.0, true);
+            pruned = (long long)alone.prune(cam, 1.0, true);
+        }
         batch.stage(0, d, W * 2, r, W * 3);
         batch.set_inputs(1, d, r);
         batch.process({1, 1});
@@ -97,7 +108,8 @@ int main() {
     const bool same = memcmp(pa.data(), p1.data(), sizeof(pa)) == 0 && memcmp(pb.data(), p1.data(), sizeof(pb)) == 0 &&
                       memcmp(res[0].pose, p1.data(), sizeof(pa)) == 0;
     const gbf_tuning t = batch.tuning();
-    printf("%d %d %lld %d %d\n", same ? 1 : 0, res[1].tracked, (long long)res[1].frame_index, t.state, t.n_tried);
+    printf("%d %d %lld %d %d %lld %lld\n", same ? 1 : 0, res[1].tracked, (long long)res[1].frame_index, t.state,
+           t.n_tried, pruned, (long long)batch.captures());
     cudaFree(depth);
     cudaFree(rgb);
     gbf_synth_destroy(sc);
@@ -128,3 +140,4 @@ def test_cpp_batch_serves_like_single_sessions(tmp_path):
     assert out[0] == "1", "batched and single-session poses differ"
     assert out[1] == "1" and out[2] == "24"
     assert int(out[3]) in (1, 2) and int(out[4]) >= 1  # the tuner explored (and may have settled)
+    assert int(out[5]) > 0 and int(out[6]) >= 2  # the prune removed blocks; graphs were captured
