@@ -337,6 +337,26 @@ GBF_API gbf_status gbf_map_write_dump(gbf_session *s, const char *path, const gb
  * Synchronises. */
 GBF_API gbf_status gbf_map_read_dump(gbf_session *s, const char *path);
 
+/* ---- session snapshot: evict to host memory, resume --------------------------- */
+/* No counterpart in the reference, which keeps one map per process and dumps only
+ * its map storage (MapStruct::writeToDisk, src/data_struct/map_struct.cu:534-613).
+ * A snapshot holds what a session's next frame reads: its allocated blocks in the
+ * session's own voxel layout (block ids kept), its pose and tracking state (the
+ * motion prior included), its counters and status bits, and the reference frame's
+ * pyramid (the raycast prediction's vertex and normal maps, the intensities).
+ * Restored into a session created with the same configuration and intrinsics (and
+ * the same library version), the session continues exactly as the original would
+ * have: the same poses and the same map, bit for bit.  Take a snapshot between
+ * frames (for a staggered batch, after gbf_batch_flush); dst / src may be host or
+ * device memory.  All three synchronise. */
+GBF_API gbf_status gbf_session_snapshot_bytes(gbf_session *s, int64_t *bytes);
+/* *written (may be NULL) = the snapshot's size; GBF_ERR_CAPACITY when capacity is smaller. */
+GBF_API gbf_status gbf_session_snapshot(gbf_session *s, void *dst, int64_t capacity, int64_t *written,
+                                        void *stream);
+/* GBF_ERR_INVALID_ARG when src is not a snapshot of this library version, or was
+ * taken from a session of another configuration or intrinsics. */
+GBF_API gbf_status gbf_session_restore(gbf_session *s, const void *src, int64_t bytes, void *stream);
+
 /* ---- block garbage collection ------------------------------------------------- */
 /* deleteBlock (src/data_struct/map_struct.cu:327-363) for a list of blocks: their
  * voxels and table entries go, the pool is compacted (the kept blocks above the

@@ -154,6 +154,34 @@ class _Session:
     def reset(self, stream=None) -> None:
         call("gbf_session_reset", self._h, _stream(stream))
 
+    def snapshot_bytes(self) -> int:
+        n = C.c_int64()
+        call("gbf_session_snapshot_bytes", self._h, C.byref(n))
+        return int(n.value)
+
+    def snapshot(self, out=None, stream=None):
+        """Everything the session's next frame reads (blocks, tracking state,
+        reference pyramid), into `out` (a host numpy uint8 array or a CUDA
+        uint8 tensor, large enough) or a new host array; returns it, cut to the
+        snapshot's size."""
+        n = self.snapshot_bytes()
+        if out is None:
+            out = np.empty(n, np.uint8)
+        ptr = out.ctypes.data if isinstance(out, np.ndarray) else out.data_ptr()
+        cap = out.nbytes if isinstance(out, np.ndarray) else out.numel() * out.element_size()
+        written = C.c_int64()
+        call("gbf_session_snapshot", self._h, ptr, cap, C.byref(written), _stream(stream))
+        return out[:int(written.value)]
+
+    def restore(self, snap, stream=None) -> None:
+        """Continue from a snapshot of a session of the same configuration and intrinsics."""
+        if isinstance(snap, np.ndarray):
+            snap = np.ascontiguousarray(snap)
+            ptr, n = snap.ctypes.data, snap.nbytes
+        else:
+            ptr, n = snap.data_ptr(), snap.numel() * snap.element_size()
+        call("gbf_session_restore", self._h, ptr, n, _stream(stream))
+
 
 class DenseMapping(_Session):
     """Voxel-hashed TSDF map (include/voxel_hashing/voxel_hashing.h:12-51)."""

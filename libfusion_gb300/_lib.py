@@ -138,6 +138,9 @@ SIGNATURES = {
     "gbf_map_delete_blocks": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_int64)]),
     "gbf_map_prune": (C.c_int, [_P, _P, C.c_double, _I32, C.POINTER(C.c_int64)]),
     "gbf_map_prune_async": (C.c_int, [_P, _P, C.c_double, _I32, _P]),
+    "gbf_session_snapshot_bytes": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "gbf_session_snapshot": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_int64), _P]),
+    "gbf_session_restore": (C.c_int, [_P, _P, _I64, _P]),
     "gbf_map_read_dump": (C.c_int, [_P, C.c_char_p]),
     "gbf_visible_blocks": (C.c_int, [_P, _P, _I64, C.POINTER(C.c_int64)]),
     "gbf_zrange": (C.c_int, [_P, _P, _I64]),

@@ -17,7 +17,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libgbfusion.so"
-SOURCES = ["runtime.cu", "ingest.cu", "mapping.cu", "raycast.cu", "tracking.cu", "mesh.cu", "synth.cu", "persist.cu", "render.cu", "gc.cu"]
+SOURCES = ["runtime.cu", "ingest.cu", "mapping.cu", "raycast.cu", "tracking.cu", "mesh.cu", "synth.cu", "persist.cu", "render.cu", "gc.cu", "snapshot.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",

@@ -37,6 +37,8 @@ int reduce_ctas(int pixels);
 int reduce_tile(int level);
 // empty the session's map (table, pool, counters) but keep its pose and tracking state; synchronises
 gbf_status reset_map(gbf_session *s);
+// clear the table and insert every pool block [0, used) at its own id (gc.cu)
+void rebuild_table(gbf_session *s, cudaStream_t st);
 
 }  // namespace gbf
 

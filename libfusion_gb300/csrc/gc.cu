@@ -199,6 +199,29 @@ __global__ void gc_insert_kernel(const SessionView *__restrict__ svs, const int 
     }
 }
 
+// every pool block [0, used) into the cleared table at its own id (a restored snapshot)
+__global__ void insert_all_kernel(const SessionView *__restrict__ svs) {
+    const SessionView &sv = svs[0];
+    const int n = used_blocks(sv);
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x) {
+        const int4 c = sv.bcoord[id];
+        const unsigned long long key = pack_key(c.x, c.y, c.z);
+        int slot = home_slot(sv, c.x, c.y, c.z);
+        bool placed = false;
+        for (int p = 0; p < sv.max_probe && !placed; ++p) {
+            HashSlot *e = sv.table + slot;
+            if (atomicCAS(&e->key, kEmptyKey, key) == kEmptyKey) {
+                e->ptr = id;
+                sv.bcoord[id].w = slot;
+                placed = true;
+            } else {
+                slot = (slot + 1 == sv.cap) ? 0 : slot + 1;
+            }
+        }
+        if (!placed) raise_flag(sv, GBF_FLAG_HASH_FULL);
+    }
+}
+
 __global__ void gc_finish_kernel(const SessionView *__restrict__ svs, const int *pre) {
     const SessionView &sv = svs[0];
     const int n = used_blocks(sv);
@@ -258,6 +281,13 @@ gbf_status deleted_count(gbf_session *s, cudaStream_t st, int64_t *n_deleted, co
 }
 
 }  // namespace
+
+void rebuild_table(gbf_session *s, cudaStream_t st) {
+    gc_clear_table_kernel<<<grid_for(s->cfg.num_buckets, kGcThreads), kGcThreads, 0, st>>>(s->view.table,
+                                                                                        s->cfg.num_buckets);
+    insert_all_kernel<<<grid_for(s->cfg.num_blocks, kGcThreads), kGcThreads, 0, st>>>(s->d_view);
+}
+
 }  // namespace gbf
 
 using namespace gbf;
