@@ -24,6 +24,14 @@ session, `collect(session, pose, stream)` runs between two ticks with the pose
 its last frame tracked -- typically gbf_map_prune_async around the camera,
 stream-ordered with the batch's launches and with no host synchronisation.
 
+Parking (optional): a camera may pause (Request.pauses: after frame k, no frame
+for that many seconds).  A session whose next frame is more than `park_after`
+seconds away is snapshotted to host memory (`snapshot(session)`, e.g.
+gbf_session_snapshot), and its slot and arena are freed for other requests;
+when its next frame arrives it is resumed -- ahead of new requests -- into a
+free slot and an arena of its configuration (`restore(session, snapshot)`,
+e.g. gbf_session_restore) and continues bit for bit.
+
 The clock, the batch and the session factory are parameters, so the scheduling
 is testable without a GPU.
 """
@@ -46,6 +54,7 @@ class Request:
     pose0: object = None           # initial camera -> world pose
     source: object = None          # frame k -> (depth device pointer, rgb device pointer)
     fps: float = 30.0
+    pauses: dict = None            # frame k -> seconds without frames after frame k
 
 
 @dataclass
@@ -56,6 +65,8 @@ class _Live:
     next_frame: int = 0
     fused: int = 0
     failed: int = 0
+    delay: float = 0.0             # pauses before next_frame
+    snapshot: object = None        # while parked
 
 
 class WallClock:
@@ -140,10 +151,15 @@ class Server:
 
     def __init__(self, batch, slots: int, cache: ArenaCache, clock=None, set_pose=None, stream=None,
                  use_graph: bool = True, look_ahead: int = 8, record_poses: bool = False, collect=None,
-                 collect_every: int = 0):
+                 collect_every: int = 0, park_after: float | None = None, snapshot=None, restore=None):
         self.batch, self.slots, self.cache = batch, slots, cache
         self.collect, self.collect_every = collect, collect_every
         self.collections = 0
+        self.park_after, self.snapshot, self.restore = park_after, snapshot, restore
+        self.parked: list[_Live] = []             # snapshotted, waiting for their next frame
+        self.parks = self.resumes = 0
+        self.snapshot_bytes = 0
+        self.park_s = self.resume_s = 0.0
         self.clock = clock or WallClock()
         self.set_pose = set_pose or (lambda s, T: s.set_pose(T))
         self.stream, self.use_graph, self.look_ahead = stream, use_graph, look_ahead
@@ -170,6 +186,43 @@ class Server:
     def _arrive(self, now: float) -> None:
         while self.pending and self.t0 + self.pending[0].arrival <= now:
             self.queue.append(self.pending.pop(0))
+
+    def _resume(self, now: float) -> None:
+        """Parked sessions whose next frame has arrived, back into free slots."""
+        for x in sorted(self.parked, key=lambda x: self._frame_time(x, x.next_frame)):
+            if self._frame_time(x, x.next_frame) > now:
+                break
+            free = [i for i, y in enumerate(self.live) if y is None]
+            if not free or not self.cache.fits(x.req.nbytes, x.req.key):
+                break
+            s = self.cache.acquire(x.req.key, x.req.nbytes)
+            if s is None:
+                break
+            t = time.perf_counter()
+            self.restore(s, x.snapshot)
+            self.resume_s += time.perf_counter() - t
+            x.session, x.snapshot = s, None
+            self.parked.remove(x)
+            slot = free[0]
+            self.batch.set(slot, s)
+            self.live[slot] = x
+            self.resumes += 1
+
+    def _park(self, now: float) -> None:
+        """Snapshot the sessions whose next frame is more than park_after away."""
+        for slot, x in enumerate(self.live):
+            if x is None or self._frame_time(x, x.next_frame) - now <= self.park_after:
+                continue
+            t = time.perf_counter()
+            x.snapshot = self.snapshot(x.session)
+            self.park_s += time.perf_counter() - t
+            self.snapshot_bytes += len(x.snapshot)
+            self.batch.set(slot, None)
+            self.cache.release(x.req.key, x.req.nbytes, x.session)
+            x.session = None
+            self.live[slot] = None
+            self.parked.append(x)
+            self.parks += 1
 
     def _admit(self, now: float) -> None:
         while self.queue:
@@ -202,7 +255,8 @@ class Server:
             self.concurrency_peak = max(self.concurrency_peak, n)
 
     def _frame_time(self, x: _Live, k: int) -> float:
-        return x.admitted + k / x.req.fps
+        """Capture time of frame k >= next_frame - 1 (pauses before next_frame counted)."""
+        return x.admitted + k / x.req.fps + x.delay
 
     def _evict(self, slot: int) -> None:
         x = self.live[slot]
@@ -214,6 +268,7 @@ class Server:
     def next_event(self) -> float | None:
         """The earliest time something can happen: an arrival or a frame."""
         ts = [self._frame_time(x, x.next_frame) for x in self.live if x is not None]
+        ts += [self._frame_time(x, x.next_frame) for x in self.parked]
         if self.pending:
             ts.append(self.t0 + self.pending[0].arrival)
         return min(ts) if ts else None
@@ -226,6 +281,8 @@ class Server:
         if self.t0 is None:
             self.t0 = now
         self._arrive(now)
+        if self.parked:
+            self._resume(now)
         self._admit(now)
         ready = [i for i, x in enumerate(self.live)
                  if x is not None and self._frame_time(x, x.next_frame) <= now]
@@ -251,6 +308,8 @@ class Server:
             if x.next_frame > 0 and not tracked[i]:
                 x.failed += 1
                 self.failed_frames += 1
+            if x.req.pauses and x.next_frame in x.req.pauses:
+                x.delay += x.req.pauses[x.next_frame]
             x.next_frame += 1
             x.fused += 1
             if x.next_frame >= x.req.frames:
@@ -258,6 +317,8 @@ class Server:
             elif self.collect is not None and self.collect_every > 0 and x.fused % self.collect_every == 0:
                 self.collect(x.session, poses[i], self.stream)
                 self.collections += 1
+        if self.park_after is not None:
+            self._park(self.clock.now())
         return True
 
     def run(self, until: float) -> None:
@@ -277,7 +338,7 @@ class Server:
         frames = len(self.latency_ms)
         wall = getattr(self, "wall", None)
         return {
-            "requests_arrived": self.completed + live + len(self.queue),
+            "requests_arrived": self.completed + live + len(self.queue) + len(self.parked),
             "admitted": len(self.queue_wait_s), "completed": self.completed, "still_serving": live,
             "still_queued": len(self.queue),
             "deferred_by_memory": len(self.deferred_memory), "deferred_by_slots": len(self.deferred_slots),
@@ -294,6 +355,9 @@ class Server:
                            "max": max(self.latency_ms) if self.latency_ms else None},
             "tracking_failed_frames": self.failed_frames,
             "collections": self.collections,
+            "parking": {"parked": self.parks, "resumed": self.resumes, "still_parked": len(self.parked),
+                        "snapshot_bytes": self.snapshot_bytes, "snapshot_s": self.park_s,
+                        "restore_s": self.resume_s},
             "memory": {"budget_bytes": self.cache.budget, "peak_bytes": self.cache.peak_bytes,
                        "arenas_created": self.cache.created, "arenas_reused": self.cache.reused,
                        "arenas_freed": self.cache.freed},

@@ -138,3 +138,52 @@ def test_restore_refuses_other_configurations_and_damaged_snapshots(gbf):
     assert e.value.status == 4  # GBF_ERR_CAPACITY
     b.restore(snap)  # the intact snapshot still restores
     assert b.stats().allocated_blocks == a.stats().allocated_blocks
+
+
+def test_server_parks_a_paused_session_and_resumes_it_bit_for_bit(gbf):
+    """The server with one slot and memory for one arena: camera 0 pauses after
+    its fourth frame, its session is snapshotted to host memory and its arena
+    goes to camera 1, which arrives during the pause and runs to its end in the
+    same arena; camera 0 then resumes in that arena again.  Every frame's pose
+    of both cameras equals the same frames run alone."""
+    import torch
+    from libfusion_gb300.serving import ArenaCache, Request, Server
+    L = gbf
+    K = H.intrinsics(L)
+    cfg = H.small_config(L, 2)
+    nbytes = L.session_bytes(cfg, K)
+    spec = [(0, 0.0, 8, 21, {3: 0.4}), (1, 0.08, 5, 22, None)]  # sid, arrival, frames, seed, pauses
+    frames = {}
+    for sid, _, n, seed, _ in spec:
+        sc = L.SynthScene(seed=seed)
+        d = torch.empty((n, K.height, K.width), dtype=torch.uint16, device="cuda")
+        c = torch.empty((n, K.height, K.width, 3), dtype=torch.uint8, device="cuda")
+        for k in range(n):
+            sc.render_into(K, k, d[k].data_ptr(), c[k].data_ptr())
+        frames[sid] = (d, c, sc.pose(0))
+        sc.close()
+    torch.cuda.synchronize()
+    batch = L.FusionBatch(1)
+    cache = ArenaCache(nbytes, make=lambda key: L.System(K, cfg), destroy=lambda s: s.close(),
+                       reset=lambda s: s.reset())
+    srv = Server(batch, 1, cache, record_poses=True, park_after=0.05, snapshot=lambda s: s.snapshot(),
+                 restore=lambda s, snap: s.restore(snap))
+    for sid, t, n, _, pauses in spec:
+        d, c, T0 = frames[sid]
+        srv.submit(Request(sid=sid, arrival=t, frames=n, key=("a",), nbytes=nbytes, pose0=T0, fps=100.0,
+                           pauses=pauses, source=lambda k, d=d, c=c: (d[k].data_ptr(), c[k].data_ptr())))
+    srv.run(5.0)
+    rep = srv.report()
+    assert rep["completed"] == 2 and rep["frames"] == 13
+    assert rep["parking"]["parked"] == 1 and rep["parking"]["resumed"] == 1
+    assert rep["memory"]["arenas_created"] == 1 and rep["tracking_failed_frames"] == 0
+    batch.close()
+    cache.close()
+    for sid, _, n, _, _ in spec:
+        d, c, T0 = frames[sid]
+        s = L.System(K, cfg)
+        s.set_pose(T0)
+        for k in range(n):
+            s.process_images(d[k], c[k])
+            assert np.array_equal(s.get_camera_pose(), srv.poses[(sid, k)]), (sid, k)
+        s.close()

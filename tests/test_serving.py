@@ -194,3 +194,31 @@ def test_collection_runs_every_n_frames_between_ticks_with_the_tracked_pose():
     assert r["collections"] == 2
     assert [c[1] for c in calls] == [4, 8]
     assert [c[3] for c in calls] == [4.0, 8.0] and all(c[2] == 0.0 and c[4] == "st" for c in calls)
+
+
+def test_a_paused_camera_parks_its_session_and_resumes_it_in_a_freed_slot():
+    clock = FakeClock()
+    batch = FakeBatch(clock, 1)
+    restored = []
+
+    def snapshot(s):
+        return bytes(10)
+
+    srv = Server(batch, 1, make_cache(100), clock=clock, set_pose=lambda s, T: None, park_after=0.2,
+                 snapshot=snapshot, restore=lambda s, snap: restored.append((s.id, len(snap))))
+    paused = req(0, 0.0, frames=6)
+    paused.pauses = {2: 1.0}  # after its third frame the camera stops for a second
+    srv.submit(paused)
+    srv.submit(req(1, 0.2, frames=10))  # arrives during the pause: takes the freed slot
+    srv.run(0.6)
+    r = srv.report()
+    assert r["parking"]["parked"] == 1 and r["parking"]["still_parked"] == 1
+    assert r["admitted"] == 2 and r["completed"] == 1 and r["frames"] == 3 + 10
+    srv.run(3.0)
+    r = srv.report()
+    assert r["completed"] == 2 and r["frames"] == 16
+    assert r["parking"]["resumed"] == 1 and r["parking"]["snapshot_bytes"] == 10 and len(restored) == 1
+    # the resumed frames were fused when they arrived (a free slot was waiting)
+    assert r["latency_ms"]["max"] < 10.0
+    # only one slot: request 1 ran while request 0 was parked, never beside it
+    assert all(len(t) == 1 for t in batch.ticks)
