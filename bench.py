@@ -1102,6 +1102,23 @@ def run_scale(args):
     collection = {"kind": "gbf_map_prune_async, blocks farther than 3 m from the last camera",
                   "blocks_before": st.allocated_blocks, "blocks_after": s.stats().allocated_blocks,
                   "ms": a3.elapsed_time(b3)}
+    # evict to host and resume: the pruned session snapshotted into pinned host
+    # memory and restored into a fresh session (host wall clock, both synchronise)
+    nb = s.snapshot_bytes()
+    host = torch.empty(nb, dtype=torch.uint8, pin_memory=True).numpy()
+    t0 = time.perf_counter()
+    s.snapshot(out=host)
+    t1 = time.perf_counter()
+    r = L.System(K, cfg)
+    t2 = time.perf_counter()
+    r.restore(host)
+    t3 = time.perf_counter()
+    snapshot = {"blocks": s.stats().allocated_blocks, "bytes": nb, "snapshot_ms": (t1 - t0) * 1e3,
+                "restore_ms": (t3 - t2) * 1e3, "snapshot_gbs": nb / (t1 - t0) / 1e9,
+                "restore_gbs": nb / (t3 - t2) / 1e9, "host_memory": "pinned",
+                "same_pose": bool(np.array_equal(r.get_camera_pose(), s.get_camera_pose()))}
+    r.close()
+    del host
     s.close()
     total_ms = sum(frame_ms) + sum(mesh_ms)
     poses = np.array(poses)
@@ -1173,6 +1190,7 @@ def run_scale(args):
         "work_per_frame": {k: v / n for k, v in work.items() if k in ("pixel_iterations", "integrated_blocks")},
         "map": {"allocated_blocks": st.allocated_blocks, "status": st.status},
         "collection": collection,
+        "snapshot": snapshot,
         "tracking": {"failed_frames": failed, "ate_vs_ground_truth_mm": float(np.sqrt(np.mean(err ** 2)) * 1e3),
                      "max_error_mm": float(err.max() * 1e3)},
         "clocks": clocks.summary(),
