@@ -348,7 +348,9 @@ GBF_API gbf_status gbf_map_read_dump(gbf_session *s, const char *path);
  * the same library version), the session continues exactly as the original would
  * have: the same poses and the same map, bit for bit.  Take a snapshot between
  * frames (for a staggered batch, after gbf_batch_flush); dst / src may be host or
- * device memory.  All three synchronise. */
+ * device memory.  All three synchronise: snapshot_bytes with the whole device,
+ * snapshot and restore with `stream`, which must be ordered after the session's
+ * last frame. */
 GBF_API gbf_status gbf_session_snapshot_bytes(gbf_session *s, int64_t *bytes);
 /* *written (may be NULL) = the snapshot's size; GBF_ERR_CAPACITY when capacity is smaller. */
 GBF_API gbf_status gbf_session_snapshot(gbf_session *s, void *dst, int64_t capacity, int64_t *written,

@@ -296,6 +296,9 @@ extern "C" {
 
 GBF_API gbf_status gbf_map_delete_blocks(gbf_session *s, const int32_t *coords, int64_t n, int64_t *n_deleted) {
     if (!s || n < 0 || (n > 0 && !coords)) return set_error(GBF_ERR_INVALID_ARG, "gbf_map_delete_blocks: null");
+    // the synchronous form: after everything queued on the device, on any stream
+    cudaError_t e0 = cudaDeviceSynchronize();
+    if (e0 != cudaSuccess) return cuda_error(e0, "gbf_map_delete_blocks");
     cudaStream_t st = nullptr;
     const int pool = s->cfg.num_blocks;
     gc_keep_all_kernel<<<grid_for(pool, kGcThreads), kGcThreads, 0, st>>>(s->d_view, s->view.mesh_off);
@@ -326,6 +329,9 @@ GBF_API gbf_status gbf_map_prune_async(gbf_session *s, const double center[3], d
 GBF_API gbf_status gbf_map_prune(gbf_session *s, const double center[3], double radius, int32_t drop_unobserved,
                                  int64_t *n_deleted) {
     if (!s) return set_error(GBF_ERR_INVALID_ARG, "gbf_map_prune: null");
+    // the synchronous form: after everything queued on the device, on any stream
+    cudaError_t e0 = cudaDeviceSynchronize();
+    if (e0 != cudaSuccess) return cuda_error(e0, "gbf_map_prune");
     cudaStream_t st = nullptr;
     mark(s, center, radius, drop_unobserved, st);
     collect(s, st);

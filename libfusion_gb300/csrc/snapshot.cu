@@ -100,6 +100,8 @@ extern "C" {
 
 GBF_API gbf_status gbf_session_snapshot_bytes(gbf_session *s, int64_t *bytes) {
     if (!s || !bytes) return set_error(GBF_ERR_INVALID_ARG, "gbf_session_snapshot_bytes: null");
+    cudaError_t e = cudaDeviceSynchronize();  // the pool end after every queued frame
+    if (e != cudaSuccess) return cuda_error(e, "gbf_session_snapshot_bytes");
     int64_t n = 0;
     gbf_status st = used_blocks_host(s, nullptr, &n, nullptr, "gbf_session_snapshot_bytes");
     if (st != GBF_OK) return st;
