@@ -129,6 +129,13 @@ void or_render_scene(const float *vmap, const float *nmap, const uint8_t *rgb, i
 /* Column sums of an n x width float matrix, sequentially down each column in
  * float: plain (kahan = 0) or compensated (Kahan 1965, kahan = 1). */
 void or_sum_f32(const float *terms, long long n, int width, int kahan, double *out);
+/* sinf / expf of the FP32 oracle, from an installed table of device values or libm */
+float or_sinf(float x);
+float or_expf(float x);
+void or_trans_record(int enable);
+long long or_trans_recorded(int kind, uint32_t *out, long long cap);
+void or_trans_table(int kind, const uint32_t *x, const float *y, long long n);
+long long or_trans_misses(int kind);
 int or_edge_table(int cube);
 short or_pack_sdf(float v);
 float or_unpack_sdf(short v);

@@ -114,6 +114,14 @@ def lib() -> C.CDLL:
         L.or_render_scene.argtypes = [P, P, P, C.c_int, C.c_int, P]
         L.or_sum_f32.restype = None
         L.or_sum_f32.argtypes = [P, C.c_longlong, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.or_trans_record.restype = None
+        L.or_trans_record.argtypes = [C.c_int]
+        L.or_trans_recorded.restype = C.c_longlong
+        L.or_trans_recorded.argtypes = [C.c_int, P, C.c_longlong]
+        L.or_trans_table.restype = None
+        L.or_trans_table.argtypes = [C.c_int, P, P, C.c_longlong]
+        L.or_trans_misses.restype = C.c_longlong
+        L.or_trans_misses.argtypes = [C.c_int]
         _lib = L
     return _lib
 
@@ -345,6 +353,67 @@ class OracleSystem:
 REF_VOXEL = np.dtype([("sdf", "<i2"), ("pad0", "<i2"), ("weight", "<f4"), ("rgb", "u1", 3), ("pad1", "u1")])
 REF_ENTRY = np.dtype([("ptr", "<i4"), ("offset", "<i4"), ("pos", "<i4", 3)])
 REF_DEFAULT_SIZE = (200000, 250000, 200000)  # MapStruct() defaults, map_struct.cu:19-21
+
+
+TRANS_SIN, TRANS_EXP = 0, 1
+
+
+def trans_record(enable: bool) -> None:
+    """Start (clearing) or stop recording the FP32 oracle's sinf / expf arguments."""
+    lib().or_trans_record(1 if enable else 0)
+
+
+def trans_recorded(kind: int) -> np.ndarray:
+    """The recorded arguments of one kind, unique, as float32."""
+    L = lib()
+    n = L.or_trans_recorded(kind, None, 0)
+    out = np.empty(n, np.uint32)
+    if n:
+        L.or_trans_recorded(kind, out.ctypes.data, n)
+    return np.unique(out).view(np.float32)
+
+
+def trans_table(kind: int, x: np.ndarray | None = None, y: np.ndarray | None = None) -> None:
+    """Install the values y = f(x) for the FP32 oracle's sinf (kind 0) or expf
+    (kind 1); None removes the table.  x: unique float32 arguments."""
+    L = lib()
+    if x is None:
+        L.or_trans_table(kind, None, None, 0)
+        return
+    xb = np.ascontiguousarray(np.asarray(x, np.float32)).view(np.uint32)
+    order = np.argsort(xb, kind="stable")
+    xs = np.ascontiguousarray(xb[order])
+    ys = np.ascontiguousarray(np.asarray(y, np.float32)[order])
+    L.or_trans_table(kind, xs.ctypes.data, ys.ctypes.data, len(xs))
+
+
+def trans_misses(kind: int) -> int:
+    return int(lib().or_trans_misses(kind))
+
+
+def with_device_transcendentals(run, device_fns):
+    """run() twice: once recording the FP32 oracle's transcendental arguments,
+    then with device_fns[kind](x) -> y (the device's sinf / expf of those
+    arguments) installed as tables.  Returns the second run's result and the
+    table sizes; the tables are removed afterwards.  The oracle's own
+    arithmetic is unchanged: only the two functions' values come from the device."""
+    trans_record(True)
+    try:
+        run()
+    finally:
+        trans_record(False)
+    sizes = {}
+    for kind, fn in device_fns.items():
+        x = trans_recorded(kind)
+        sizes[kind] = len(x)
+        trans_table(kind, x, fn(x) if len(x) else x)
+    try:
+        out = run()
+        misses = {k: trans_misses(k) for k in device_fns}
+    finally:
+        for kind in device_fns:
+            trans_table(kind, None)
+    return out, sizes, misses
 
 
 def parse_ref_dump(path) -> dict:

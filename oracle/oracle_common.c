@@ -4,6 +4,9 @@
  */
 #include <limits.h>
 #include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "oracle.h"
 
@@ -149,3 +152,96 @@ void or_sum_f32(const float *terms, long long n, int width, int kahan, double *o
         out[k] = (double)s;
     }
 }
+
+/* Transcendental tables.  The reference's weighted integration and bilateral
+ * filter call CUDA's sinf and expf, whose last bits differ from libm's.  For a
+ * bit-for-bit comparison a test may hand the FP32 oracle the device's values
+ * for exactly the arguments the oracle evaluates: it records the arguments of
+ * one run (or_trans_record), has the device evaluate them, installs the pairs
+ * (or_trans_table) and runs again.  Every other operation stays the oracle's
+ * own; an argument missing from an installed table falls back to libm and is
+ * counted (or_trans_misses).  Kind 0: sinf, kind 1: expf. */
+typedef struct {
+    uint32_t *x;  /* argument bit patterns, ascending */
+    float *y;
+    long long n;
+    long long misses;
+} OrTransTable;
+static OrTransTable g_trans[2];
+static uint32_t *g_rec[2];
+static long long g_rec_n[2], g_rec_cap[2];
+static int g_recording;
+
+static uint32_t f2u(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    return u;
+}
+
+static float trans_eval(int kind, float x) {
+    if (g_recording) {
+#pragma omp critical(or_trans_record)
+        {
+            if (g_rec_n[kind] == g_rec_cap[kind]) {
+                const long long cap = g_rec_cap[kind] ? 2 * g_rec_cap[kind] : 1 << 16;
+                uint32_t *p = (uint32_t *)realloc(g_rec[kind], (size_t)cap * sizeof(uint32_t));
+                if (p) {
+                    g_rec[kind] = p;
+                    g_rec_cap[kind] = cap;
+                }
+            }
+            if (g_rec_n[kind] < g_rec_cap[kind]) g_rec[kind][g_rec_n[kind]++] = f2u(x);
+        }
+    }
+    const OrTransTable *t = &g_trans[kind];
+    if (t->n > 0) {
+        const uint32_t key = f2u(x);
+        long long lo = 0, hi = t->n - 1;
+        while (lo <= hi) {
+            const long long mid = (lo + hi) / 2;
+            if (t->x[mid] == key) return t->y[mid];
+            if (t->x[mid] < key) lo = mid + 1;
+            else hi = mid - 1;
+        }
+#pragma omp atomic
+        g_trans[kind].misses++;
+    }
+    return kind == 0 ? sinf(x) : expf(x);
+}
+
+float or_sinf(float x) { return trans_eval(0, x); }
+float or_expf(float x) { return trans_eval(1, x); }
+
+/* enable: clear the recorded arguments and start recording; 0: stop (they are kept) */
+void or_trans_record(int enable) {
+    if (enable)
+        for (int k = 0; k < 2; ++k) g_rec_n[k] = 0;
+    g_recording = enable ? 1 : 0;
+}
+
+long long or_trans_recorded(int kind, uint32_t *out, long long cap) {
+    if (kind < 0 || kind > 1) return -1;
+    if (out) memcpy(out, g_rec[kind], (size_t)(cap < g_rec_n[kind] ? cap : g_rec_n[kind]) * sizeof(uint32_t));
+    return g_rec_n[kind];
+}
+
+/* x ascending (unique bit patterns); n = 0 removes the table */
+void or_trans_table(int kind, const uint32_t *x, const float *y, long long n) {
+    if (kind < 0 || kind > 1) return;
+    OrTransTable *t = &g_trans[kind];
+    free(t->x);
+    free(t->y);
+    t->x = NULL;
+    t->y = NULL;
+    t->n = 0;
+    t->misses = 0;
+    if (n <= 0) return;
+    t->x = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+    t->y = (float *)malloc((size_t)n * sizeof(float));
+    if (!t->x || !t->y) return;
+    memcpy(t->x, x, (size_t)n * sizeof(uint32_t));
+    memcpy(t->y, y, (size_t)n * sizeof(float));
+    t->n = n;
+}
+
+long long or_trans_misses(int kind) { return (kind == 0 || kind == 1) ? g_trans[kind].misses : -1; }

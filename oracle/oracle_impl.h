@@ -37,8 +37,8 @@ typedef double R;
 typedef float R;
 #define SFX(n) n##_f32
 #define RSQRT sqrtf
-#define RSIN sinf
-#define REXP expf
+#define RSIN or_sinf
+#define REXP or_expf
 #define RFABS fabsf
 #define RFLOOR floorf
 #define RCEIL ceilf

@@ -12,6 +12,10 @@ tree; this script runs there.  It prints, per case, whether the oracle on the
 same machine matches, and writes the fixture (default gpurun_out/, to be
 copied into tests/golden/).
 
+It also stores CUDA's sinf of every argument the oracle's normal-weighted
+update evaluates on these frames (sin_x, sin_y), recorded from the oracle and
+evaluated on the GPU, so that the pin test can compare that update bit for bit.
+
 Usage: python tests/golden/make_kernel_golden.py [OUT.npz]
 """
 from __future__ import annotations
@@ -431,7 +435,13 @@ def main() -> None:
         poses.append(sc.pose(k))
     sc.close()
     dep, rgb, poses = np.stack(dep), np.stack(rgb), np.stack(poses)
+    # the oracle's sinf arguments (the normal-weighted update), recorded, with
+    # CUDA's sinf of each: the pin test installs them as the oracle's table
+    O.trans_record(True)
     oc = P.oracle_states(L, O, dep, rgb, poses)
+    O.trans_record(False)
+    sin_x = O.trans_recorded(O.TRANS_SIN)
+    sin_y = torch.sin(torch.from_numpy(sin_x).cuda()).cpu().numpy()
 
     exact = Reference("")
     exact.set_state("fusion", 1 << 15, 1 << 14, 1 << 13)
@@ -445,7 +455,7 @@ def main() -> None:
     print(json.dumps(report, indent=1))
 
     fx = {"depth_u16": dep, "rgb": rgb, "poses": poses, "frame_digest": np.array(P.frame_digest(
-        P.oracle_frames(L, O, dep, rgb)))}
+        P.oracle_frames(L, O, dep, rgb))), "sin_x": sin_x, "sin_y": sin_y}
     for k in ("s1", "s2_colour", "s2_weighted"):
         coords, code, w, c = got[k]
         chosen = P.choose_subset(coords)

@@ -16,10 +16,12 @@ with every float operation rounded as written
 (tests/golden/make_kernel_golden.py; cases in tests/golden/pin_cases.py).
 
 CPU tests: the oracle recomputes every case from the stored frames.  Integer
-and float results are compared bit for bit, except the normal-weighted update,
-whose weight |sin(n_z)| / d^2 takes CUDA's sinf in the reference and libm's in
-the oracle (a few ulp apart): there the sdf codes may differ by one
-truncation step and the colours by one level, on a small share of the voxels.
+and float results are compared bit for bit.  The normal-weighted update's
+weight |sin(n_z)| / d^2 takes CUDA's sinf in the reference and libm's in the
+oracle (a few ulp apart): with the fixture's table of CUDA's sinf for the
+arguments the oracle evaluates it matches bit for bit too; with libm's sinf the
+sdf codes may differ by one truncation step and the colours by one level, on
+a small share of the voxels.
 
 GPU tests: the CUDA kernels on the same inputs match the reference's outputs
 bit for bit, the normal-weighted update included (both use CUDA's sinf), and
@@ -83,6 +85,28 @@ def test_colour_integration_bit_exact(fx, states, case):
     assert np.array_equal(w[idx].view(np.int32), fx[f"{case}_subset_weight"].view(np.int32))
     assert np.array_equal(rgb[idx], fx[f"{case}_subset_rgb"])
     assert P.digest(coords, code, w, rgb) == str(fx[f"{case}_digest"]), "voxels outside the stored subset differ"
+
+
+def test_weighted_integration_bit_exact_with_device_sinf(fx, lib, oracle_mod):
+    """With CUDA's sinf values for the arguments it evaluates (stored in the
+    fixture by its generator), the oracle's normal-weighted update equals the
+    reference kernel's output bit for bit."""
+    O = oracle_mod
+    assert len(fx["sin_x"]) > 1000
+    O.trans_table(O.TRANS_SIN, fx["sin_x"], fx["sin_y"])
+    try:
+        st = P.oracle_states(lib, O, *frames(fx))
+        misses = O.trans_misses(O.TRANS_SIN)
+    finally:
+        O.trans_table(O.TRANS_SIN)
+    assert misses == 0, "an argument the generator did not record"
+    coords, code, w, rgb = st["s2_weighted"]
+    assert np.array_equal(coords, fx["s2_weighted_coords"])
+    idx = P.subset_rows(coords, fx["s2_weighted_subset"])
+    assert np.array_equal(code[idx], fx["s2_weighted_subset_code"])
+    assert np.array_equal(w[idx].view(np.int32), fx["s2_weighted_subset_weight"].view(np.int32))
+    assert np.array_equal(rgb[idx], fx["s2_weighted_subset_rgb"])
+    assert P.digest(coords, code, w, rgb) == str(fx["s2_weighted_digest"]), "voxels outside the stored subset differ"
 
 
 def test_weighted_integration_within_sinf_rounding(fx, states):
