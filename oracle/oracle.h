@@ -132,6 +132,7 @@ void or_sum_f32(const float *terms, long long n, int width, int kahan, double *o
 /* sinf / expf of the FP32 oracle, from an installed table of device values or libm */
 float or_sinf(float x);
 float or_expf(float x);
+float or_powf20(float x);
 void or_trans_record(int enable);
 long long or_trans_recorded(int kind, uint32_t *out, long long cap);
 void or_trans_table(int kind, const uint32_t *x, const float *y, long long n);

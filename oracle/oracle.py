@@ -355,7 +355,7 @@ REF_ENTRY = np.dtype([("ptr", "<i4"), ("offset", "<i4"), ("pos", "<i4", 3)])
 REF_DEFAULT_SIZE = (200000, 250000, 200000)  # MapStruct() defaults, map_struct.cu:19-21
 
 
-TRANS_SIN, TRANS_EXP = 0, 1
+TRANS_SIN, TRANS_EXP, TRANS_POW20 = 0, 1, 2
 
 
 def trans_record(enable: bool) -> None:

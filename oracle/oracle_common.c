@@ -99,6 +99,8 @@ static uint8_t sat255(float v) {
     return (uint8_t)(s * 255.f);
 }
 
+float or_powf20(float x);
+
 static void render_point(F3 p, F3 n, F3 img, F3 light, uint8_t out[4]) {
     float c0 = 4.f / 255.f, c1 = 2.f / 255.f, c2 = 2.f / 255.f;
     if (!(p.x != p.x)) {
@@ -112,7 +114,8 @@ static void render_point(F3 p, F3 n, F3 img, F3 light, uint8_t out[4]) {
         const int tx = or_trunc_sat(n.x * 2.f), ty = or_trunc_sat(n.y * 2.f), tz = or_trunc_sat(n.z * 2.f);
         const F3 R = f3_normalised(f3((float)tx * nl - L.x, (float)ty * nl - L.y, (float)tz * nl - L.z));
         const float rv = f3_dot(R, V);
-        const float Ix = ((Ax * Ka) * Dx + ((Lx * Kd) * Dx) * fmaxf(0.f, nl)) + ((Lx * Ks) * Sx) * powf(fmaxf(0.f, rv), sp);
+        (void)sp;  /* the exponent, 20: or_powf20 */
+        const float Ix = ((Ax * Ka) * Dx + ((Lx * Kd) * Dx) * fmaxf(0.f, nl)) + ((Lx * Ks) * Sx) * or_powf20(fmaxf(0.f, rv));
         c0 = c1 = c2 = Ix;
     }
     out[0] = sat255(c0);
@@ -160,16 +163,18 @@ void or_sum_f32(const float *terms, long long n, int width, int kahan, double *o
  * one run (or_trans_record), has the device evaluate them, installs the pairs
  * (or_trans_table) and runs again.  Every other operation stays the oracle's
  * own; an argument missing from an installed table falls back to libm and is
- * counted (or_trans_misses).  Kind 0: sinf, kind 1: expf. */
+ * counted (or_trans_misses).  Kind 0: sinf, kind 1: expf, kind 2: powf(x, 20)
+ * (the shading's specular term). */
 typedef struct {
     uint32_t *x;  /* argument bit patterns, ascending */
     float *y;
     long long n;
     long long misses;
 } OrTransTable;
-static OrTransTable g_trans[2];
-static uint32_t *g_rec[2];
-static long long g_rec_n[2], g_rec_cap[2];
+#define OR_TRANS_KINDS 3
+static OrTransTable g_trans[OR_TRANS_KINDS];
+static uint32_t *g_rec[OR_TRANS_KINDS];
+static long long g_rec_n[OR_TRANS_KINDS], g_rec_cap[OR_TRANS_KINDS];
 static int g_recording;
 
 static uint32_t f2u(float x) {
@@ -206,28 +211,29 @@ static float trans_eval(int kind, float x) {
 #pragma omp atomic
         g_trans[kind].misses++;
     }
-    return kind == 0 ? sinf(x) : expf(x);
+    return kind == 0 ? sinf(x) : kind == 1 ? expf(x) : powf(x, 20.f);
 }
 
 float or_sinf(float x) { return trans_eval(0, x); }
 float or_expf(float x) { return trans_eval(1, x); }
+float or_powf20(float x) { return trans_eval(2, x); }
 
 /* enable: clear the recorded arguments and start recording; 0: stop (they are kept) */
 void or_trans_record(int enable) {
     if (enable)
-        for (int k = 0; k < 2; ++k) g_rec_n[k] = 0;
+        for (int k = 0; k < OR_TRANS_KINDS; ++k) g_rec_n[k] = 0;
     g_recording = enable ? 1 : 0;
 }
 
 long long or_trans_recorded(int kind, uint32_t *out, long long cap) {
-    if (kind < 0 || kind > 1) return -1;
+    if (kind < 0 || kind >= OR_TRANS_KINDS) return -1;
     if (out) memcpy(out, g_rec[kind], (size_t)(cap < g_rec_n[kind] ? cap : g_rec_n[kind]) * sizeof(uint32_t));
     return g_rec_n[kind];
 }
 
 /* x ascending (unique bit patterns); n = 0 removes the table */
 void or_trans_table(int kind, const uint32_t *x, const float *y, long long n) {
-    if (kind < 0 || kind > 1) return;
+    if (kind < 0 || kind >= OR_TRANS_KINDS) return;
     OrTransTable *t = &g_trans[kind];
     free(t->x);
     free(t->y);
@@ -244,4 +250,4 @@ void or_trans_table(int kind, const uint32_t *x, const float *y, long long n) {
     t->n = n;
 }
 
-long long or_trans_misses(int kind) { return (kind == 0 || kind == 1) ? g_trans[kind].misses : -1; }
+long long or_trans_misses(int kind) { return (kind >= 0 && kind < OR_TRANS_KINDS) ? g_trans[kind].misses : -1; }

@@ -46,11 +46,19 @@ def test_raycast_check_visibility_bit_exact(gbf, layout):
         assert np.array_equal(g[gh], o[oh])
 
 
+def _device_pow20(x):
+    """CUDA's powf(x, 20.f) of float32 arguments (a float32 tensor-tensor pow)."""
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
+    return torch.pow(t, torch.full_like(t, 20.0)).cpu().numpy()
+
+
 def test_render_scene_matches_oracle(gbf):
-    """Shaded model prediction of a System session, plain and textured.  Every
-    step but powf rounds as written on both sides; CUDA's powf and the host
-    libm's may differ in the last bits, which can move a truncated 8-bit value by
-    one on rare pixels."""
+    """Shaded model prediction of a System session, plain and textured, bit for
+    bit: every step rounds as written on both sides, and the oracle takes
+    CUDA's powf(x, 20) for the bases it evaluates (recorded in a first run).
+    With libm's powf instead, a truncated 8-bit value may move by one on rare
+    pixels, which the second check bounds."""
     import oracle as O
     import torch
     L = gbf
@@ -68,6 +76,10 @@ def test_render_scene_matches_oracle(gbf):
     rgb = fr[-1][1]
     for textured in (False, True):
         g = (s.get_rendered_scene_textured() if textured else s.get_rendered_image()).cpu().numpy()
+        exact, sizes, misses = O.with_device_transcendentals(
+            lambda: O.render_scene(v, n, rgb if textured else None), {O.TRANS_POW20: _device_pow20})
+        assert sizes[O.TRANS_POW20] > 1000 and misses[O.TRANS_POW20] == 0
+        assert np.array_equal(g, exact)
         o = O.render_scene(v, n, rgb if textured else None)
         diff = np.abs(g.astype(np.int32) - o.astype(np.int32))
         assert diff.max() <= 1
