@@ -9,8 +9,8 @@ device modules oracle/_ref/pin_*.cubin, which oracle/ref_pin/build_kernels.sh
 compiles from the reference sources where they lie.  The modules are built
 where the reference tree is and carried to the GPU machine with the working
 tree; this script runs there.  It prints, per case, whether the oracle on the
-same machine matches, and writes the fixture (default gpurun_out/, to be
-copied into tests/golden/).
+same machine matches, and writes the fixture (default
+tests/golden/ref_kernels.npz).
 
 It also stores CUDA's sinf of every argument the oracle's normal-weighted
 update evaluates on these frames (sin_x, sin_y), recorded from the oracle and
@@ -416,7 +416,7 @@ def contraction_report(a: dict, b: dict) -> dict:
 
 def main() -> None:
     import torch
-    out_path = Path(sys.argv[1]) if len(sys.argv) > 1 else ROOT / "gpurun_out" / "ref_kernels.npz"
+    out_path = Path(sys.argv[1]) if len(sys.argv) > 1 else ROOT / "tests" / "golden" / "ref_kernels.npz"
     assert torch.cuda.is_available(), "needs a CUDA GPU"
     torch.zeros(1, device="cuda")  # the primary context, current on this thread
     from libfusion_gb300 import build as B
