@@ -126,6 +126,17 @@ __device__ __forceinline__ float read_vox(const SV &sv, BlockCache &bc, int vx, 
     return __int_as_float(0x7fffffff);
 }
 
+// Voxel (vx, vy, vz) of block id (looked up by the caller): sdf, or NaN when
+// the block is unallocated (id < 0) or the voxel unobserved.
+template <int LAYOUT, class SV>
+__device__ __forceinline__ float vox_in(const SV &sv, int id, int vx, int vy, int vz, bool &valid) {
+    if (id >= 0)
+        return sdf_at<LAYOUT>(sv, id * kBlockVoxels + (voxel_to_local(vz) * 64 + voxel_to_local(vy) * 8 +
+                                                       voxel_to_local(vx)), valid);
+    valid = false;
+    return __int_as_float(0x7fffffff);
+}
+
 // read_sdf (ray_tracing.cu:291-305): nearest voxel ToVector3i(pt)
 template <int LAYOUT, class SV>
 __device__ __forceinline__ float read_sdf(const SV &sv, BlockCache &bc, float px, float py, float pz,
@@ -177,29 +188,43 @@ __device__ __forceinline__ float read_sdf_interped(const SV &sv, BlockCache &bc,
         valid = vpt && v1 && v2 && v3 && v4 && v5 && v6 && v7;
         return (1.0f - fz) * r2 + fz * r3;
     }
+    // The corners span two to eight blocks.  Each distinct block is looked up
+    // once: read corner by corner through the one-block cache, the corners
+    // alternate between the blocks and the same blocks would be looked up again.
+    const int bx0 = voxel_to_block(x0), bx1 = voxel_to_block(x1), by0 = voxel_to_block(y0),
+              by1 = voxel_to_block(y1), bz0 = voxel_to_block(z0), bz1 = voxel_to_block(z1);
+    const bool sx = bx1 != bx0, sy = by1 != by0, sz = bz1 != bz0;
+    const int i000 = bc.get(sv, bx0, by0, bz0);
+    const int i100 = sx ? find_block(sv, bx1, by0, bz0) : i000;
+    const int i010 = sy ? find_block(sv, bx0, by1, bz0) : i000;
+    const int i110 = (sx && sy) ? find_block(sv, bx1, by1, bz0) : (sx ? i100 : i010);
+    const int i001 = sz ? find_block(sv, bx0, by0, bz1) : i000;
+    const int i101 = sz ? (sx ? find_block(sv, bx1, by0, bz1) : i001) : i100;
+    const int i011 = sz ? (sy ? find_block(sv, bx0, by1, bz1) : i001) : i010;
+    const int i111 = sz ? ((sx && sy) ? find_block(sv, bx1, by1, bz1) : (sx ? i101 : i011)) : i110;
     if (HAVE000) {
         s0 = s000;
         vpt = v000;
     } else {
-        s0 = read_vox<LAYOUT>(sv, bc, x0, y0, z0, vpt);
+        s0 = vox_in<LAYOUT>(sv, i000, x0, y0, z0, vpt);
     }
-    s1 = read_vox<LAYOUT>(sv, bc, x1, y0, z0, v);
+    s1 = vox_in<LAYOUT>(sv, i100, x1, y0, z0, v);
     vpt &= v;
     r0 = (1.0f - fx) * s0 + fx * s1;
-    s0 = read_vox<LAYOUT>(sv, bc, x0, y1, z0, v);
+    s0 = vox_in<LAYOUT>(sv, i010, x0, y1, z0, v);
     vpt &= v;
-    s1 = read_vox<LAYOUT>(sv, bc, x1, y1, z0, v);
+    s1 = vox_in<LAYOUT>(sv, i110, x1, y1, z0, v);
     vpt &= v;
     r1 = (1.0f - fx) * s0 + fx * s1;
     r2 = (1.0f - fy) * r0 + fy * r1;
-    s0 = read_vox<LAYOUT>(sv, bc, x0, y0, z1, v);
+    s0 = vox_in<LAYOUT>(sv, i001, x0, y0, z1, v);
     vpt &= v;
-    s1 = read_vox<LAYOUT>(sv, bc, x1, y0, z1, v);
+    s1 = vox_in<LAYOUT>(sv, i101, x1, y0, z1, v);
     vpt &= v;
     r0 = (1.0f - fx) * s0 + fx * s1;
-    s0 = read_vox<LAYOUT>(sv, bc, x0, y1, z1, v);
+    s0 = vox_in<LAYOUT>(sv, i011, x0, y1, z1, v);
     vpt &= v;
-    s1 = read_vox<LAYOUT>(sv, bc, x1, y1, z1, v);
+    s1 = vox_in<LAYOUT>(sv, i111, x1, y1, z1, v);
     vpt &= v;
     r1 = (1.0f - fx) * s0 + fx * s1;
     r3 = (1.0f - fy) * r0 + fy * r1;
