@@ -144,6 +144,56 @@ __device__ __forceinline__ float read_sdf(const SV &sv, BlockCache &bc, float px
     return read_vox<LAYOUT>(sv, bc, floor_ref(px), floor_ref(py), floor_ref(pz), valid);
 }
 
+// The trilinear read when the corners span two to eight blocks (about 1/3 of
+// the reads): out of line, so that the march loop's code stays small.  i000:
+// the block of corner (x0, y0, z0), looked up by the caller.
+template <int LAYOUT, class SV>
+__device__ __noinline__ float interp_spanning(const SV sv, int i000, int x0, int x1, int y0, int y1, int z0, int z1,
+                                              float fx, float fy, float fz, float s000, bool v000, bool have000,
+                                              bool &valid) {
+    const int bx0 = voxel_to_block(x0), bx1 = voxel_to_block(x1), by0 = voxel_to_block(y0),
+              by1 = voxel_to_block(y1), bz0 = voxel_to_block(z0), bz1 = voxel_to_block(z1);
+    const bool sx = bx1 != bx0, sy = by1 != by0, sz = bz1 != bz0;
+    const int i100 = sx ? find_block(sv, bx1, by0, bz0) : i000;
+    const int i010 = sy ? find_block(sv, bx0, by1, bz0) : i000;
+    const int i110 = (sx && sy) ? find_block(sv, bx1, by1, bz0) : (sx ? i100 : i010);
+    const int i001 = sz ? find_block(sv, bx0, by0, bz1) : i000;
+    const int i101 = sz ? (sx ? find_block(sv, bx1, by0, bz1) : i001) : i100;
+    const int i011 = sz ? (sy ? find_block(sv, bx0, by1, bz1) : i001) : i010;
+    const int i111 = sz ? ((sx && sy) ? find_block(sv, bx1, by1, bz1) : (sx ? i101 : i011)) : i110;
+    bool vpt, v;
+    float s0, s1, r0, r1, r2, r3;
+    if (have000) {
+        s0 = s000;
+        vpt = v000;
+    } else {
+        s0 = vox_in<LAYOUT>(sv, i000, x0, y0, z0, vpt);
+    }
+    s1 = vox_in<LAYOUT>(sv, i100, x1, y0, z0, v);
+    vpt &= v;
+    r0 = (1.0f - fx) * s0 + fx * s1;
+    s0 = vox_in<LAYOUT>(sv, i010, x0, y1, z0, v);
+    vpt &= v;
+    s1 = vox_in<LAYOUT>(sv, i110, x1, y1, z0, v);
+    vpt &= v;
+    r1 = (1.0f - fx) * s0 + fx * s1;
+    r2 = (1.0f - fy) * r0 + fy * r1;
+    s0 = vox_in<LAYOUT>(sv, i001, x0, y0, z1, v);
+    vpt &= v;
+    s1 = vox_in<LAYOUT>(sv, i101, x1, y0, z1, v);
+    vpt &= v;
+    r0 = (1.0f - fx) * s0 + fx * s1;
+    s0 = vox_in<LAYOUT>(sv, i011, x0, y1, z1, v);
+    vpt &= v;
+    s1 = vox_in<LAYOUT>(sv, i111, x1, y1, z1, v);
+    vpt &= v;
+    r1 = (1.0f - fx) * s0 + fx * s1;
+    r3 = (1.0f - fy) * r0 + fy * r1;
+    valid = vpt;
+    return (1.0f - fz) * r2 + fz * r3;
+}
+
+
 // read_sdf_interped (ray_tracing.cu:307-339).  The reference reads the eight
 // corners at pt + (0|1, 0|1, 0|1) and floors each sum; the six per-axis floors
 // floor(p), floor(p + 1) are computed once (floor(p + 1) is not always
@@ -158,8 +208,8 @@ __device__ __forceinline__ float read_sdf_interped(const SV &sv, BlockCache &bc,
     const int x0 = floor_ref(px + 0.0f), x1 = floor_ref(px + 1.0f);
     const int y0 = floor_ref(py + 0.0f), y1 = floor_ref(py + 1.0f);
     const int z0 = floor_ref(pz + 0.0f), z1 = floor_ref(pz + 1.0f);
-    bool vpt, v;
-    float s0, s1, r0, r1, r2, r3;
+    bool vpt;
+    float r0, r1, r2, r3;
     if (x1 == x0 + 1 && y1 == y0 + 1 && z1 == z0 + 1 && (x0 & 7) != 7 && (y0 & 7) != 7 && (z0 & 7) != 7) {
         const int id = bc.get(sv, voxel_to_block(x0), voxel_to_block(y0), voxel_to_block(z0));
         if (id < 0) {  // every corner unallocated: the general path's NaN arithmetic, invalid
@@ -188,48 +238,8 @@ __device__ __forceinline__ float read_sdf_interped(const SV &sv, BlockCache &bc,
         valid = vpt && v1 && v2 && v3 && v4 && v5 && v6 && v7;
         return (1.0f - fz) * r2 + fz * r3;
     }
-    // The corners span two to eight blocks.  Each distinct block is looked up
-    // once: read corner by corner through the one-block cache, the corners
-    // alternate between the blocks and the same blocks would be looked up again.
-    const int bx0 = voxel_to_block(x0), bx1 = voxel_to_block(x1), by0 = voxel_to_block(y0),
-              by1 = voxel_to_block(y1), bz0 = voxel_to_block(z0), bz1 = voxel_to_block(z1);
-    const bool sx = bx1 != bx0, sy = by1 != by0, sz = bz1 != bz0;
-    const int i000 = bc.get(sv, bx0, by0, bz0);
-    const int i100 = sx ? find_block(sv, bx1, by0, bz0) : i000;
-    const int i010 = sy ? find_block(sv, bx0, by1, bz0) : i000;
-    const int i110 = (sx && sy) ? find_block(sv, bx1, by1, bz0) : (sx ? i100 : i010);
-    const int i001 = sz ? find_block(sv, bx0, by0, bz1) : i000;
-    const int i101 = sz ? (sx ? find_block(sv, bx1, by0, bz1) : i001) : i100;
-    const int i011 = sz ? (sy ? find_block(sv, bx0, by1, bz1) : i001) : i010;
-    const int i111 = sz ? ((sx && sy) ? find_block(sv, bx1, by1, bz1) : (sx ? i101 : i011)) : i110;
-    if (HAVE000) {
-        s0 = s000;
-        vpt = v000;
-    } else {
-        s0 = vox_in<LAYOUT>(sv, i000, x0, y0, z0, vpt);
-    }
-    s1 = vox_in<LAYOUT>(sv, i100, x1, y0, z0, v);
-    vpt &= v;
-    r0 = (1.0f - fx) * s0 + fx * s1;
-    s0 = vox_in<LAYOUT>(sv, i010, x0, y1, z0, v);
-    vpt &= v;
-    s1 = vox_in<LAYOUT>(sv, i110, x1, y1, z0, v);
-    vpt &= v;
-    r1 = (1.0f - fx) * s0 + fx * s1;
-    r2 = (1.0f - fy) * r0 + fy * r1;
-    s0 = vox_in<LAYOUT>(sv, i001, x0, y0, z1, v);
-    vpt &= v;
-    s1 = vox_in<LAYOUT>(sv, i101, x1, y0, z1, v);
-    vpt &= v;
-    r0 = (1.0f - fx) * s0 + fx * s1;
-    s0 = vox_in<LAYOUT>(sv, i011, x0, y1, z1, v);
-    vpt &= v;
-    s1 = vox_in<LAYOUT>(sv, i111, x1, y1, z1, v);
-    vpt &= v;
-    r1 = (1.0f - fx) * s0 + fx * s1;
-    r3 = (1.0f - fy) * r0 + fy * r1;
-    valid = vpt;
-    return (1.0f - fz) * r2 + fz * r3;
+    const int i000 = bc.get(sv, voxel_to_block(x0), voxel_to_block(y0), voxel_to_block(z0));
+    return interp_spanning<LAYOUT>(sv, i000, x0, x1, y0, y1, z0, z1, fx, fy, fz, s000, v000, HAVE000, valid);
 }
 
 // The fields the march reads on every step, copied into registers once per
