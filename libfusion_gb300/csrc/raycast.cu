@@ -10,10 +10,13 @@
 //             are positive) of every covered cell.  The reference's 16x16
 //             rendering-tile list, its cudaMalloc and its host read-back
 //             (:223-277) are gone; the union of its tiles is exactly the box.
-//   raycast   one thread per pixel, warps on 16x2 pixel strips; the march of
-//             MapRenderingDelegate::operator() (:346-425) with a per-thread cache
-//             of the last block lookup so trilinear samples within one block
-//             cost one hash probe.  Output: camera-frame float4 vertex (NaN = miss).
+//   raycast   one thread per pixel, 64-pixel CTAs (8x8 by default: a warp is
+//             an 8x4 patch);
+//             the march of MapRenderingDelegate::operator() (:346-425) with a
+//             per-thread cache of the last block lookup, so trilinear samples
+//             within one block cost one hash probe; a trilinear read spanning
+//             blocks looks each block up once, out of line.  Output:
+//             camera-frame float4 vertex (NaN = miss).
 //   post      2x2 mean vertex pyramid, then normals of every level.
 #include "gbf_device.cuh"
 #include "gbf_kernels.h"
