@@ -248,11 +248,11 @@ class ClockSampler:
 # pixel-iterations, dram__bytes_read.sum + dram__bytes_write.sum): the roofline's traffic
 REDUCE_DRAM_BYTES_PER_PIXEL_ITER = (102.178048e6 + 3.364608e6) / 1228800
 # DRAM bytes per raycast pixel, from one ncu capture of the SNORM raycast over 4
-# sessions (66.26 MB read + 4.59 MB written for 4 x 307,200 pixels; same
-# counters), and its issue-active fraction there.  The bytes depend on the maps
-# the rays cross, so scaling by pixels is an estimate.
-RAYCAST_DRAM_BYTES_PER_PIXEL = (66.264576e6 + 4.589312e6) / (4 * 307200)
-RAYCAST_ISSUE_ACTIVE = 0.759
+# sessions with maps of 96 fused frames (81.94 MB read + 12.55 MB written for
+# 4 x 307,200 pixels; same counters), and its issue-active fraction there.  The
+# bytes depend on the maps the rays cross, so scaling by pixels is an estimate.
+RAYCAST_DRAM_BYTES_PER_PIXEL = (81.93536e6 + 12.553472e6) / (4 * 307200)
+RAYCAST_ISSUE_ACTIVE = 0.744
 
 
 def measured_peaks():
@@ -732,9 +732,9 @@ def run_ours(args):
                                  "times this run's pixel-iterations per launch" if traffic is not None else None,
                 "work_per_step": {"pixel_iterations": pix_iter, "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
                 "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream",
-                "why_this_kernel": "the raycast (39% of launch time against the reduction's 32% in an ncu "
+                "why_this_kernel": "the raycast (37% of launch time against the reduction's 33% in an ncu "
                                    "launch list of the 64-session tick) is bound by instruction issue, not HBM "
-                                   "(76% issue active, DRAM 2.6% in its ncu capture at 4 sessions), so its "
+                                   "(74% issue active, DRAM 3.8% in its ncu capture at 4 sessions), so its "
                                    "figures are under 'march'; the HBM roofline is given for the memory-bound phase",
                 "march_ms_per_step": phases["march"]}
     px_step = sum(s.K.width * s.K.height for s in sessions)
