@@ -66,6 +66,8 @@ void launch_march(const SessionView *d_sv, int nslots, const Extent &ex, float4 
 // computeNMapK (cuda_imgproc.cu:276-305) of a pitched vertex map into a pitched normal map
 void launch_nmap_of(const float4 *vmap, long long vmap_pitch, float4 *nmap, long long nmap_pitch, int w, int h,
                     cudaStream_t st);
+// kernel launches of one launch_post
+int post_launches(const Extent &ex);
 void launch_post(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st);
 
 // ---- tracking (tracking.cu) -----------------------------------------------------

@@ -383,17 +383,112 @@ __global__ void vmap_down_kernel(const SessionView *__restrict__ svs, int level)
 // `stride` float4 apart: normalised cross product of the horizontal and vertical
 // differences; NaN in the last row and column (written, where the reference
 // leaves them unwritten) and wherever a neighbour is NaN.
-__device__ __forceinline__ float4 normal_at(const float4 *V, long long stride, int x, int y, int w, int h) {
+template <class Get>
+__device__ __forceinline__ float4 normal_by(const Get &V, int x, int y, int w, int h) {
     const float qnan = __int_as_float(0x7fffffff);
     if (x >= w - 1 || y >= h - 1) return make_float4(qnan, qnan, qnan, qnan);
     const int x10 = max(x - 1, 0), y10 = max(y - 1, 0);
-    const float4 v00 = V[y * stride + x10], v01 = V[y * stride + x + 1];
-    const float4 v10 = V[y10 * stride + x], v11 = V[(y + 1) * stride + x];
+    const float4 v00 = V(x10, y), v01 = V(x + 1, y);
+    const float4 v10 = V(x, y10), v11 = V(x, y + 1);
     const float3 a = make_float3(v01.x - v00.x, v01.y - v00.y, v01.z - v00.z);
     const float3 bb = make_float3(v11.x - v10.x, v11.y - v10.y, v11.z - v10.z);
     const float3 n = cross3(a, bb);
     const float l = norm3(n.x, n.y, n.z);
     return make_float4(n.x / l, n.y / l, n.z / l, 1.f);
+}
+__device__ __forceinline__ float4 normal_at(const float4 *V, long long stride, int x, int y, int w, int h) {
+    return normal_by([&](int xx, int yy) { return V[yy * stride + xx]; }, x, y, w, h);
+}
+
+// 2x2 mean of four vertices in vmap_down_kernel's order
+__device__ __forceinline__ float4 mean4(const float4 a, const float4 b, const float4 c, const float4 d) {
+    return make_float4((((a.x + b.x) + c.x) + d.x) * 0.25f, (((a.y + b.y) + c.y) + d.y) * 0.25f,
+                       (((a.z + b.z) + c.z) + d.z) * 0.25f, (((a.w + b.w) + c.w) + d.w) * 0.25f);
+}
+
+// The post-raycast pyramid of up to three levels in one pass: a CTA takes a
+// 32x32 tile of the level-0 vertex map with a 4-pixel halo into shared memory,
+// writes the tile's level-0 normals, builds the 16x16 level-1 tile (2x2 means,
+// vmap_down_kernel's arithmetic) with a 2-pixel halo and its normals, then the
+// 8x8 level-2 tile with a 1-pixel halo and its normals -- the arithmetic of
+// vmap_down_kernel and nmap_all_kernel, reading the level-0 map once instead of
+// writing and re-reading every level.
+constexpr int kPostTile = 32;
+__global__ void __launch_bounds__(256) post_pyramid_kernel(const SessionView *__restrict__ svs) {
+    const SessionView &sv = svs[blockIdx.y];
+    if (!sv.active) return;
+    const int w0 = sv.lv[0].w, h0 = sv.lv[0].h;
+    const int tiles_x = (w0 + kPostTile - 1) / kPostTile;
+    const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    if (ty * kPostTile >= h0) return;  // a smaller frame than the batch's largest
+    const int set = sv.ts->idx;
+    const float qnan = __int_as_float(0x7fffffff);
+    const float4 nan4 = make_float4(qnan, qnan, qnan, qnan);
+    __shared__ float4 s0[kPostTile + 8][kPostTile + 8];
+    __shared__ float4 s1[kPostTile / 2 + 4][kPostTile / 2 + 4];
+    __shared__ float4 s2[kPostTile / 4 + 2][kPostTile / 4 + 2];
+    // level 0: the tile and its 4-pixel halo (outside the image: never read)
+    const int ox0 = tx * kPostTile - 4, oy0 = ty * kPostTile - 4;
+    const float4 *V0 = sv.vmap[set][0];
+    for (int i = threadIdx.x; i < (kPostTile + 8) * (kPostTile + 8); i += blockDim.x) {
+        const int lx = i % (kPostTile + 8), ly = i / (kPostTile + 8), x = ox0 + lx, y = oy0 + ly;
+        s0[ly][lx] = (x >= 0 && y >= 0 && x < w0 && y < h0) ? V0[(size_t)y * w0 + x] : nan4;
+    }
+    __syncthreads();
+    {
+        const auto get0 = [&](int x, int y) { return s0[y - oy0][x - ox0]; };
+        float4 *N0 = sv.nmap[set][0];
+        for (int i = threadIdx.x; i < kPostTile * kPostTile; i += blockDim.x) {
+            const int x = tx * kPostTile + i % kPostTile, y = ty * kPostTile + i / kPostTile;
+            if (x < w0 && y < h0) N0[(size_t)y * w0 + x] = normal_by(get0, x, y, w0, h0);
+        }
+    }
+    if (sv.levels < 2) return;
+    // level 1: the 16x16 tile and a 2-pixel halo, from the level-0 pixels in s0
+    const int w1 = sv.lv[1].w, h1 = sv.lv[1].h;
+    const int ox1 = tx * (kPostTile / 2) - 2, oy1 = ty * (kPostTile / 2) - 2;
+    float4 *V1 = sv.vmap[set][1];
+    for (int i = threadIdx.x; i < (kPostTile / 2 + 4) * (kPostTile / 2 + 4); i += blockDim.x) {
+        const int lx = i % (kPostTile / 2 + 4), ly = i / (kPostTile / 2 + 4), x = ox1 + lx, y = oy1 + ly;
+        float4 v = nan4;
+        if (x >= 0 && y >= 0 && x < w1 && y < h1) {
+            // level-0 pixel (2x, 2y) sits at s0[2 ly][2 lx]
+            v = mean4(s0[2 * ly][2 * lx], s0[2 * ly][2 * lx + 1], s0[2 * ly + 1][2 * lx], s0[2 * ly + 1][2 * lx + 1]);
+            if (lx >= 2 && ly >= 2 && lx < kPostTile / 2 + 2 && ly < kPostTile / 2 + 2) V1[(size_t)y * w1 + x] = v;
+        }
+        s1[ly][lx] = v;
+    }
+    __syncthreads();
+    {
+        const auto get1 = [&](int x, int y) { return s1[y - oy1][x - ox1]; };
+        float4 *N1 = sv.nmap[set][1];
+        for (int i = threadIdx.x; i < (kPostTile / 2) * (kPostTile / 2); i += blockDim.x) {
+            const int x = tx * (kPostTile / 2) + i % (kPostTile / 2), y = ty * (kPostTile / 2) + i / (kPostTile / 2);
+            if (x < w1 && y < h1) N1[(size_t)y * w1 + x] = normal_by(get1, x, y, w1, h1);
+        }
+    }
+    if (sv.levels < 3) return;
+    // level 2: the 8x8 tile and a 1-pixel halo, from the level-1 pixels in s1
+    const int w2 = sv.lv[2].w, h2 = sv.lv[2].h;
+    const int ox2 = tx * (kPostTile / 4) - 1, oy2 = ty * (kPostTile / 4) - 1;
+    float4 *V2 = sv.vmap[set][2];
+    for (int i = threadIdx.x; i < (kPostTile / 4 + 2) * (kPostTile / 4 + 2); i += blockDim.x) {
+        const int lx = i % (kPostTile / 4 + 2), ly = i / (kPostTile / 4 + 2), x = ox2 + lx, y = oy2 + ly;
+        float4 v = nan4;
+        if (x >= 0 && y >= 0 && x < w2 && y < h2) {
+            // level-1 pixel (2x, 2y) sits at s1[2 ly][2 lx]
+            v = mean4(s1[2 * ly][2 * lx], s1[2 * ly][2 * lx + 1], s1[2 * ly + 1][2 * lx], s1[2 * ly + 1][2 * lx + 1]);
+            if (lx >= 1 && ly >= 1 && lx < kPostTile / 4 + 1 && ly < kPostTile / 4 + 1) V2[(size_t)y * w2 + x] = v;
+        }
+        s2[ly][lx] = v;
+    }
+    __syncthreads();
+    const auto get2 = [&](int x, int y) { return s2[y - oy2][x - ox2]; };
+    float4 *N2 = sv.nmap[set][2];
+    for (int i = threadIdx.x; i < (kPostTile / 4) * (kPostTile / 4); i += blockDim.x) {
+        const int x = tx * (kPostTile / 4) + i % (kPostTile / 4), y = ty * (kPostTile / 4) + i / (kPostTile / 4);
+        if (x < w2 && y < h2) N2[(size_t)y * w2 + x] = normal_by(get2, x, y, w2, h2);
+    }
 }
 
 __global__ void nmap_of_kernel(const float4 *vmap, long long vmap_pitch, float4 *nmap, long long nmap_pitch, int w,
@@ -462,7 +557,14 @@ void launch_nmap_of(const float4 *vmap, long long vmap_pitch, float4 *nmap, long
     nmap_of_kernel<<<dim3((w + 127) / 128, h), 128, 0, st>>>(vmap, vmap_pitch, nmap, nmap_pitch, w, h);
 }
 
+int post_launches(const Extent &ex) { return ex.levels <= 3 ? 1 : ex.levels; }
+
 void launch_post(const SessionView *d_sv, int nslots, const Extent &ex, cudaStream_t st) {
+    if (ex.levels <= 3) {
+        const int tiles = ((ex.w + kPostTile - 1) / kPostTile) * ((ex.h + kPostTile - 1) / kPostTile);
+        post_pyramid_kernel<<<dim3(tiles, nslots), 256, 0, st>>>(d_sv);
+        return;
+    }
     int w = ex.w, h = ex.h, total = (w * h + 255) / 256;
     for (int l = 1; l < ex.levels; ++l) {
         w /= 2; h /= 2;

@@ -320,7 +320,7 @@ void enqueue_frame(const SessionView *d_sv, int nslots, const Extent &ex, const 
 int kernels_per_frame(const Extent &ex, const int *layouts, int nslots) {
     int nl = 0;
     for (int l = 0; l < kNumLayouts; ++l) nl += layouts[l];
-    return (1 + (ex.levels - 1) + 1) + track_launches(nslots, ex) + 3 + nl + 2 + nl + (ex.levels - 1) + 1;
+    return (1 + (ex.levels - 1) + 1) + track_launches(nslots, ex) + 3 + nl + 2 + nl + post_launches(ex);
 }
 
 }  // namespace
