@@ -509,6 +509,16 @@ GBF_API gbf_status gbf_session_inputs(gbf_session *s, uint16_t **depth, uint8_t 
     return GBF_OK;
 }
 
+// Rows of an image into dense rows: one contiguous copy when the source rows
+// are dense too (a camera frame usually is).  A pitched copy from pinned host
+// memory measured 0.43 ms slower per 64-frame tick of the batch it overlapped
+// (64 x 640x480 depth + colour staged per tick).
+static cudaError_t copy_rows(void *dst, const void *src, int64_t src_pitch, size_t row_bytes, int rows,
+                             cudaStream_t st) {
+    if (src_pitch == (int64_t)row_bytes) return cudaMemcpyAsync(dst, src, row_bytes * (size_t)rows, cudaMemcpyDefault, st);
+    return cudaMemcpy2DAsync(dst, row_bytes, src, (size_t)src_pitch, row_bytes, rows, cudaMemcpyDefault, st);
+}
+
 GBF_API gbf_status gbf_session_stage(gbf_session *s, const uint16_t *depth, int64_t depth_pitch, const uint8_t *rgb,
                                      int64_t rgb_pitch, void *stream) {
     if (!s || !depth || !rgb) return set_error(GBF_ERR_INVALID_ARG, "gbf_session_stage: null");
@@ -516,10 +526,8 @@ GBF_API gbf_status gbf_session_stage(gbf_session *s, const uint16_t *depth, int6
     if (depth_pitch < W * 2 || rgb_pitch < W * 3)
         return set_error(GBF_ERR_INVALID_ARG, "gbf_session_stage: pitch smaller than a row");
     cudaStream_t st = (cudaStream_t)stream;
-    cudaError_t e = cudaMemcpy2DAsync(s->view.in_depth, (size_t)W * 2, depth, depth_pitch, (size_t)W * 2, H,
-                                      cudaMemcpyDefault, st);
-    if (e == cudaSuccess)
-        e = cudaMemcpy2DAsync(s->view.in_rgb, (size_t)W * 3, rgb, rgb_pitch, (size_t)W * 3, H, cudaMemcpyDefault, st);
+    cudaError_t e = copy_rows(s->view.in_depth, depth, depth_pitch, (size_t)W * 2, H, st);
+    if (e == cudaSuccess) e = copy_rows(s->view.in_rgb, rgb, rgb_pitch, (size_t)W * 3, H, st);
     return cuda_error(e, "gbf_session_stage");
 }
 
@@ -1475,12 +1483,8 @@ GBF_API gbf_status gbf_batch_stage(gbf_batch *b, int32_t slot, const uint16_t *d
     cudaStream_t st = (cudaStream_t)stream;
     // the tick two submissions back read these buffers
     if (b->ev_used[k]) e = cudaStreamWaitEvent(st, b->ev[k], 0);
-    if (e == cudaSuccess)
-        e = cudaMemcpy2DAsync(b->stg_depth[k][slot], (size_t)W * 2, depth, depth_pitch, (size_t)W * 2, H,
-                              cudaMemcpyDefault, st);
-    if (e == cudaSuccess)
-        e = cudaMemcpy2DAsync(b->stg_rgb[k][slot], (size_t)W * 3, rgb, rgb_pitch, (size_t)W * 3, H,
-                              cudaMemcpyDefault, st);
+    if (e == cudaSuccess) e = copy_rows(b->stg_depth[k][slot], depth, depth_pitch, (size_t)W * 2, H, st);
+    if (e == cudaSuccess) e = copy_rows(b->stg_rgb[k][slot], rgb, rgb_pitch, (size_t)W * 3, H, st);
     if (e == cudaSuccess) e = cudaEventRecord(b->staged_ev[k][slot], st);
     if (e != cudaSuccess) return cuda_error(e, "gbf_batch_stage");
     b->staged[k][slot] = 1;
