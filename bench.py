@@ -787,14 +787,17 @@ def run_ours(args):
     eb.results(back=0)
     torch.cuda.synchronize()
     got.clear()
-    t_e2e = time.perf_counter()
-    for k in range(warm, warm + n_e2e):
-        e2e_tick(k, warm)
-    got.append(eb.results(back=0))
-    t_e2e = time.perf_counter() - t_e2e
+    with ClockSampler(local) as e2e_clocks:
+        e2e_clocks.start()
+        t_e2e = time.perf_counter()
+        for k in range(warm, warm + n_e2e):
+            e2e_tick(k, warm)
+        got.append(eb.results(back=0))
+        t_e2e = time.perf_counter() - t_e2e
+        e2e_clocks.stop()
     assert len(got) == n_e2e
     e2e = {"value": S * world * n_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": S * W * H * 5,
-           "d2h_bytes_per_step": S * 144, "steps": n_e2e,
+           "d2h_bytes_per_step": S * 144, "steps": n_e2e, "clocks": e2e_clocks.summary(),
            "note": f"frames {warm}..{warm + n_e2e - 1} of every session after {warm} untimed warm-up frames; "
                    "host wall clock from the first staging copy to the last tick's results on the host"}
     eb.close()
