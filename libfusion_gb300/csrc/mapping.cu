@@ -228,6 +228,25 @@ __global__ void __launch_bounds__(256, 6) visible_kernel(const SessionView *svs)
 
 constexpr int kIntThreads = 128;  // threads per integration CTA (512 / kIntThreads voxels each), 16 CTAs per SM
 
+// a / b rounded to nearest, from y = 1/b rounded to nearest (__frcp_rn): the
+// quotient a*y corrected twice by the exact remainder r = a - b*q (one fused
+// multiply-add).  The first correction leaves q within one unit in the last
+// place of a/b; from such a q and the correctly rounded y, the second gives
+// the correctly rounded quotient (Markstein's theorem: P. Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990; also in J.-M. Muller et al., Handbook of Floating-Point
+// Arithmetic, on division with a fused multiply-add), barring overflow and
+// underflow, which the running means here (|a| <= 255 * 510, 0 < b <= 510,
+// nonzero |a / b| far above the subnormal range) do not reach.  a is never -0
+// here (a -0 sum needs both products -0), so the corrections keep the sign of
+// a zero quotient.  tests/test_arith_proofs.py checks the steps in exact
+// arithmetic on the running means' ranges.
+__device__ __forceinline__ float div_rn_by(float a, float b, float y) {
+    const float q0 = __fmul_rn(a, y);
+    const float q1 = __fmaf_rn(__fmaf_rn(-q0, b, a), y, q0);
+    return __fmaf_rn(__fmaf_rn(-q1, b, a), y, q1);
+}
+
 template <int LAYOUT>
 __global__ void __launch_bounds__(kIntThreads, 16) integrate_kernel(const SessionView *__restrict__ svs, int mode) {
     const SessionView &sv = svs[blockIdx.y];
@@ -299,12 +318,15 @@ __global__ void __launch_bounds__(kIntThreads, 16) integrate_kernel(const Sessio
             if (old.w == 0.f) {
                 nsdf = sdf; nw = weight; nrgb = cn;
             } else {
-                nsdf = (old.sdf * old.w + sdf * weight) / (old.w + weight);
-                nw = old.w + weight;
+                // the four running means share one denominator: one correctly
+                // rounded reciprocal, then each quotient by div_rn_by
                 const float den = old.w + weight;
-                nrgb.x = (unsigned char)__float2int_rz(((float)old.rgb.x * old.w + (float)cn.x * weight) / den);
-                nrgb.y = (unsigned char)__float2int_rz(((float)old.rgb.y * old.w + (float)cn.y * weight) / den);
-                nrgb.z = (unsigned char)__float2int_rz(((float)old.rgb.z * old.w + (float)cn.z * weight) / den);
+                const float rden = __frcp_rn(den);
+                nsdf = div_rn_by(old.sdf * old.w + sdf * weight, den, rden);
+                nw = old.w + weight;
+                nrgb.x = (unsigned char)__float2int_rz(div_rn_by((float)old.rgb.x * old.w + (float)cn.x * weight, den, rden));
+                nrgb.y = (unsigned char)__float2int_rz(div_rn_by((float)old.rgb.y * old.w + (float)cn.y * weight, den, rden));
+                nrgb.z = (unsigned char)__float2int_rz(div_rn_by((float)old.rgb.z * old.w + (float)cn.z * weight, den, rden));
                 nrgb.w = 0;
             }
             store_sw_at<LAYOUT>(vox_sw, vi, nsdf, nw);

@@ -44,3 +44,50 @@ def test_snorm_unit_round_trips():
     assert np.array_equal(np.trunc(t).astype(np.int32), k)
     assert np.array_equal(np.rint(t).astype(np.int32), k)
     assert np.abs(v).max() <= np.float32(1) + np.float32(2.0 ** -23)
+
+
+def _div_rn_by(a: Fraction, b: Fraction) -> Fraction:
+    """The integration's running-mean quotient: y = RN(1/b), q0 = RN(a y), then
+    twice q = RN(RN(a - b q) y + q) (fused multiply-adds)."""
+    y = _f32(1 / b)
+    q = _f32(a * y)
+    for _ in range(2):
+        r = _f32(a - b * q)
+        q = _f32(r * y + q)
+    return q
+
+
+def test_running_mean_division_by_shared_reciprocal():
+    """The four running means of an integration update (sdf and three colour
+    channels, depth_fusion.cu:405-426) share the denominator w_old + w_new; the
+    kernel divides each by the shared reciprocal with two remainder corrections.
+    Over the updates' ranges (weights 1e-4..255, sdf codes, colours 0..255) and
+    adversarial quotients (exact, one unit in the last place off, power-of-two
+    denominators) the result is the correctly rounded quotient."""
+    rng = np.random.default_rng(7)
+    f = np.float32
+    cases = []
+    for _ in range(6000):
+        w0 = f(10.0 ** rng.uniform(-4, np.log10(255)))
+        w1 = f(10.0 ** rng.uniform(-4, 1.7))
+        b = w0 + w1
+        if rng.random() < 0.5:
+            c0, c1 = f(rng.integers(0, 256)), f(rng.integers(0, 256))
+        else:
+            c0 = f(rng.integers(-32767, 32768)) * f(float.fromhex("0x1.000202p-15"))
+            c1 = f(min(1.0, rng.uniform(-1.2, 1.2)))
+        a = c0 * w0 + c1 * w1
+        cases.append((a, b))
+    for _ in range(1500):
+        b = f(10.0 ** rng.uniform(-3, np.log10(510)))
+        k = f(rng.integers(0, 256))
+        a = k * b
+        cases += [(a, b), (np.nextafter(a, f(np.inf)), b), (np.nextafter(a, f(0)), b)]
+        p2 = f(2.0 ** rng.integers(-8, 9))
+        cases.append((f(rng.uniform(0, 255)) * p2, p2))
+    bad = []
+    for a, b in cases:
+        A, B = Fraction(float(a)), Fraction(float(b))
+        if _div_rn_by(A, B) != _f32(A / B):
+            bad.append((float(a), float(b)))
+    assert not bad, bad[:5]
