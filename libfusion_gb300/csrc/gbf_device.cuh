@@ -93,6 +93,27 @@ __device__ __forceinline__ M34 load_m34(const float *m) {
 }
 
 // ---------------------------------------------------------------------------
+// a / b rounded to nearest, from y = 1/b rounded to nearest (__frcp_rn): the
+// quotient a*y corrected twice by the exact remainder r = a - b*q (one fused
+// multiply-add).  The first correction leaves q within one unit in the last
+// place of a/b; from such a q and the correctly rounded y, the second gives
+// the correctly rounded quotient (Markstein's theorem: P. Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990; also in J.-M. Muller et al., Handbook of Floating-Point
+// Arithmetic, on division with a fused multiply-add), barring overflow and
+// underflow.  Callers that share b between several quotients compute y once.
+// Used for the integration's four running means, which share b (|a| <= 255 *
+// 510, 0 < b <= 510, nonzero |a / b| far above the subnormal range; a is never
+// -0 there, which would need both products -0, so a zero quotient keeps its
+// sign; tests/test_arith_proofs.py checks the steps in exact arithmetic on these
+// ranges).  For two quotients sharing b (the voxel and photometric
+// projections) it measured slower than two divisions.
+__device__ __forceinline__ float div_rn_by(float a, float b, float y) {
+    const float q0 = __fmul_rn(a, y);
+    const float q1 = __fmaf_rn(__fmaf_rn(-q0, b, a), y, q0);
+    return __fmaf_rn(__fmaf_rn(-q1, b, a), y, q1);
+}
+
 // Vector3 helpers in the reference's order (include/math/vector_type.h)
 __device__ __forceinline__ float norm3(float x, float y, float z) {
     return sqrtf((x * x + y * y) + z * z);

@@ -228,25 +228,6 @@ __global__ void __launch_bounds__(256, 6) visible_kernel(const SessionView *svs)
 
 constexpr int kIntThreads = 128;  // threads per integration CTA (512 / kIntThreads voxels each), 16 CTAs per SM
 
-// a / b rounded to nearest, from y = 1/b rounded to nearest (__frcp_rn): the
-// quotient a*y corrected twice by the exact remainder r = a - b*q (one fused
-// multiply-add).  The first correction leaves q within one unit in the last
-// place of a/b; from such a q and the correctly rounded y, the second gives
-// the correctly rounded quotient (Markstein's theorem: P. Markstein, "Computation
-// of elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
-// Dev. 34(1), 1990; also in J.-M. Muller et al., Handbook of Floating-Point
-// Arithmetic, on division with a fused multiply-add), barring overflow and
-// underflow, which the running means here (|a| <= 255 * 510, 0 < b <= 510,
-// nonzero |a / b| far above the subnormal range) do not reach.  a is never -0
-// here (a -0 sum needs both products -0), so the corrections keep the sign of
-// a zero quotient.  tests/test_arith_proofs.py checks the steps in exact
-// arithmetic on the running means' ranges.
-__device__ __forceinline__ float div_rn_by(float a, float b, float y) {
-    const float q0 = __fmul_rn(a, y);
-    const float q1 = __fmaf_rn(__fmaf_rn(-q0, b, a), y, q0);
-    return __fmaf_rn(__fmaf_rn(-q1, b, a), y, q1);
-}
-
 template <int LAYOUT>
 __global__ void __launch_bounds__(kIntThreads, 16) integrate_kernel(const SessionView *__restrict__ svs, int mode) {
     const SessionView &sv = svs[blockIdx.y];
