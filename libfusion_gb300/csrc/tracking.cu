@@ -11,7 +11,9 @@
 // partials in a fixed order by compensated float addition, then its first warp
 // runs the step on the device: FP64 LDL^T solve of the 6x6 system, SE(3)
 // exponential, pose composition, and the reference's error-increase / revert /
-// break rules.  No host round trip: the
+// break rules.  Launches of 8 or more sessions take the sum and the step in a
+// launch of their own (one CTA per session) instead, so that the reduction's
+// CTAs end without a fence and a ticket; the sums and the step are the same.  No host round trip: the
 // reference pays two device->host syncs per iteration (pose_estimator.cu:302-304,
 // m_estimator.cu:477-479).  The order of every sum is fixed, so a session's
 // result does not depend on the other sessions in the batch.
@@ -560,7 +562,7 @@ __device__ __forceinline__ void sum_partials(ReduceSmem &sm, const float *parts,
 }
 
 struct ReduceArgs {
-    int level, iter, once;
+    int level, iter, once, defer;
     float pose[12];
     float stddev;
 };
@@ -606,6 +608,7 @@ __global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const Sess
     __syncthreads();
     cta_partial<true>(sm, sv, level, rs, cs, T, stddev_s, blockIdx.x, sv.red_tile[level],
                 sv.partials + (size_t)blockIdx.x * kPartialStride);
+    if (a.defer) return;  // gn_step_kernel, launched next, sums the partials and takes the step
     __threadfence();
     __syncthreads();
     __shared__ unsigned int ticket;
@@ -618,6 +621,20 @@ __global__ void __launch_bounds__(kReduceThreads, 4) gn_reduce_kernel(const Sess
     if (threadIdx.x < kReduceWidth) ts->last_sums[threadIdx.x] = total[threadIdx.x];
     if (threadIdx.x == 0) sv.ctr[C_TICKET] = 0;
     if (!a.once && threadIdx.x < 32) gn_epilogue(sv, level, a.iter, total);  // one warp
+}
+
+// The session's sum of the partial records and the Gauss-Newton step, as the
+// last CTA of gn_reduce_kernel takes them, in a launch of its own (one CTA per
+// session) after a deferred reduction: the reduction's CTAs then end without a
+// fence and a ticket.
+__global__ void __launch_bounds__(kReduceThreads) gn_step_kernel(const SessionView *__restrict__ svs, ReduceArgs a) {
+    const SessionView &sv = svs[blockIdx.x];
+    if (!session_runs(sv, a)) return;
+    __shared__ ReduceSmem sm;
+    __shared__ double total[kReduceWidth];
+    sum_partials(sm, sv.partials, sv.red_ctas[a.level], total);
+    if (threadIdx.x < kReduceWidth) sv.ts->last_sums[threadIdx.x] = total[threadIdx.x];
+    if (threadIdx.x < 32) gn_epilogue(sv, a.level, a.iter, total);
 }
 
 // Host loop body of DenseTracking::compute_transform (icp_tracker.cpp:52-139),
@@ -785,10 +802,20 @@ __global__ void track_finish_kernel(const SessionView *__restrict__ svs, int fra
 // then stay in L2 from one iteration to the next.
 constexpr int kTrackSubgroup = 64;
 
+// Sessions per launch from which the Gauss-Newton step runs as a launch of its
+// own (gn_step_kernel) instead of in the last CTA of the reduction: with many
+// sessions the reduction's CTAs then end without a fence and a ticket (64
+// sessions: track 3.71 -> 3.46 ms); with one, the extra launches cost more
+// (the one-session path: 1,236 -> 1,165 frames/s).
+constexpr int kDeferStepSessions = 8;
+bool defer_step(int sessions) { return sessions >= kDeferStepSessions; }
+
 int track_launches(int nslots, const Extent &ex) {
     int it = 0;
     for (int l = 0; l < ex.levels; ++l) it += ex.max_iter[l];
-    return 2 + ((nslots + kTrackSubgroup - 1) / kTrackSubgroup) * it;
+    int n = 0;
+    for (int s0 = 0; s0 < nslots; s0 += kTrackSubgroup) n += it * (defer_step(min(kTrackSubgroup, nslots - s0)) ? 2 : 1);
+    return 2 + n;
 }
 
 void launch_track(const SessionView *d_sv, int nslots, const Extent &ex, int frame_mode, cudaStream_t st) {
@@ -801,7 +828,9 @@ void launch_track(const SessionView *d_sv, int nslots, const Extent &ex, int fra
             for (int iter = 0; iter < ex.max_iter[level]; ++iter) {
                 a.level = level;
                 a.iter = iter;
+                a.defer = defer_step(n) ? 1 : 0;
                 gn_reduce_kernel<<<dim3(ex.max_red[level], n), kReduceThreads, 0, st>>>(d_sv + s0, a);
+                if (a.defer) gn_step_kernel<<<n, kReduceThreads, 0, st>>>(d_sv + s0, a);
             }
         }
     }
