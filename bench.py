@@ -732,7 +732,7 @@ def run_ours(args):
                                  "times this run's pixel-iterations per launch" if traffic is not None else None,
                 "work_per_step": {"pixel_iterations": pix_iter, "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
                 "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream",
-                "why_this_kernel": "the raycast (38% of launch time against the reduction's 32% in an ncu "
+                "why_this_kernel": "the raycast (39% of launch time against the reduction's 27% and its step's 4% in an ncu "
                                    "launch list of the 64-session tick) is bound by instruction issue, not HBM "
                                    "(74% issue active, DRAM 3.8% in its ncu capture at 4 sessions), so its "
                                    "figures are under 'march'; the HBM roofline is given for the memory-bound phase",
