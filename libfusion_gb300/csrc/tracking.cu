@@ -13,9 +13,9 @@
 // exponential, pose composition, and the reference's error-increase / revert /
 // break rules.  Launches of 8 or more sessions take the sum and the step in a
 // launch of their own (one CTA per session) instead, so that the reduction's
-// CTAs end without a fence and a ticket; the sums and the step are the same.  No host round trip: the
-// reference pays two device->host syncs per iteration (pose_estimator.cu:302-304,
-// m_estimator.cu:477-479).  The order of every sum is fixed, so a session's
+// CTAs end without a fence and a ticket; the sums and the step are the same.
+// No host round trip: the reference pays two device->host syncs per iteration
+// (pose_estimator.cu:302-304, m_estimator.cu:477-479).  The order of every sum is fixed, so a session's
 // result does not depend on the other sessions in the batch.
 #include <float.h>
 #include <string.h>
@@ -808,13 +808,14 @@ constexpr int kTrackSubgroup = 64;
 // sessions: track 3.71 -> 3.46 ms); with one, the extra launches cost more
 // (the one-session path: 1,236 -> 1,165 frames/s).
 constexpr int kDeferStepSessions = 8;
-bool defer_step(int sessions) { return sessions >= kDeferStepSessions; }
+static bool defer_step(int sessions) { return sessions >= kDeferStepSessions; }
 
 int track_launches(int nslots, const Extent &ex) {
     int it = 0;
     for (int l = 0; l < ex.levels; ++l) it += ex.max_iter[l];
     int n = 0;
-    for (int s0 = 0; s0 < nslots; s0 += kTrackSubgroup) n += it * (defer_step(min(kTrackSubgroup, nslots - s0)) ? 2 : 1);
+    for (int s0 = 0; s0 < nslots; s0 += kTrackSubgroup)
+        n += it * (defer_step(min(kTrackSubgroup, nslots - s0)) ? 2 : 1);
     return 2 + n;
 }
 
