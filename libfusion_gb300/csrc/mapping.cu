@@ -305,9 +305,12 @@ __global__ void __launch_bounds__(kIntThreads, 16) integrate_kernel(const Sessio
                 const float rden = __frcp_rn(den);
                 nsdf = div_rn_by(old.sdf * old.w + sdf * weight, den, rden);
                 nw = old.w + weight;
-                nrgb.x = (unsigned char)__float2int_rz(div_rn_by((float)old.rgb.x * old.w + (float)cn.x * weight, den, rden));
-                nrgb.y = (unsigned char)__float2int_rz(div_rn_by((float)old.rgb.y * old.w + (float)cn.y * weight, den, rden));
-                nrgb.z = (unsigned char)__float2int_rz(div_rn_by((float)old.rgb.z * old.w + (float)cn.z * weight, den, rden));
+                nrgb.x = (unsigned char)__float2int_rz(
+                    div_rn_by((float)old.rgb.x * old.w + (float)cn.x * weight, den, rden));
+                nrgb.y = (unsigned char)__float2int_rz(
+                    div_rn_by((float)old.rgb.y * old.w + (float)cn.y * weight, den, rden));
+                nrgb.z = (unsigned char)__float2int_rz(
+                    div_rn_by((float)old.rgb.z * old.w + (float)cn.z * weight, den, rden));
                 nrgb.w = 0;
             }
             store_sw_at<LAYOUT>(vox_sw, vi, nsdf, nw);

@@ -515,7 +515,8 @@ GBF_API gbf_status gbf_session_inputs(gbf_session *s, uint16_t **depth, uint8_t 
 // (64 x 640x480 depth + colour staged per tick).
 static cudaError_t copy_rows(void *dst, const void *src, int64_t src_pitch, size_t row_bytes, int rows,
                              cudaStream_t st) {
-    if (src_pitch == (int64_t)row_bytes) return cudaMemcpyAsync(dst, src, row_bytes * (size_t)rows, cudaMemcpyDefault, st);
+    if (src_pitch == (int64_t)row_bytes)
+        return cudaMemcpyAsync(dst, src, row_bytes * (size_t)rows, cudaMemcpyDefault, st);
     return cudaMemcpy2DAsync(dst, row_bytes, src, (size_t)src_pitch, row_bytes, rows, cudaMemcpyDefault, st);
 }
 
