@@ -11,7 +11,7 @@
 // partials in a fixed order by compensated float addition, then its first warp
 // runs the step on the device: FP64 LDL^T solve of the 6x6 system, SE(3)
 // exponential, pose composition, and the reference's error-increase / revert /
-// break rules.  Launches of 8 or more sessions take the sum and the step in a
+// break rules.  Launches of 32 or more sessions take the sum and the step in a
 // launch of their own (one CTA per session) instead, so that the reduction's
 // CTAs end without a fence and a ticket; the sums and the step are the same.
 // No host round trip: the reference pays two device->host syncs per iteration
@@ -804,10 +804,12 @@ constexpr int kTrackSubgroup = 64;
 
 // Sessions per launch from which the Gauss-Newton step runs as a launch of its
 // own (gn_step_kernel) instead of in the last CTA of the reduction: with many
-// sessions the reduction's CTAs then end without a fence and a ticket (64
-// sessions: track 3.71 -> 3.46 ms); with one, the extra launches cost more
-// (the one-session path: 1,236 -> 1,165 frames/s).
-constexpr int kDeferStepSessions = 8;
+// sessions the reduction's CTAs then end without a fence and a ticket (two
+// groups of 32 sessions: track 3.71 -> 3.46 ms, tick 10.85 -> 10.80 ms; of 64:
+// 5,950 -> 6,057 frames/s); with fewer, the extra launch per iteration costs
+// more than it saves (two groups of 16: 5,764 -> 5,702 frames/s; one session:
+// 1,236 -> 1,165 frames/s).
+constexpr int kDeferStepSessions = 32;
 static bool defer_step(int sessions) { return sessions >= kDeferStepSessions; }
 
 int track_launches(int nslots, const Extent &ex) {

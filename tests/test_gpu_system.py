@@ -107,6 +107,49 @@ def test_batch_session_isolation(gbf):
 
 
 
+
+def test_step_launch_of_a_large_batch_matches_sessions_alone(gbf):
+    """A launch of 32 or more sessions takes each session's partial-record sum
+    and Gauss-Newton step in a launch of its own (gn_step_kernel); a session
+    alone takes them in the reduction's last CTA.  32 sessions in one launch
+    give every session, frame by frame, the poses it has alone, bit for bit."""
+    import torch
+    L = gbf
+    K = H.intrinsics(L, 160, 120)
+    n, nf = 32, 4
+    fr = {seed: H.frames(L, K, nf, seed=seed) for seed in (3, 9, 11, 17)}
+    seeds = [(3, 9, 11, 17)[i % 4] for i in range(n)]
+    cfgs = [H.small_config(L, i % 3, num_blocks=1 << 13, num_buckets=1 << 15) for i in range(n)]
+
+    alone = []
+    for i in range(n):
+        s = L.System(K, cfgs[i])
+        s.set_pose(fr[seeds[i]][0][2])
+        poses = []
+        for d, c, _ in fr[seeds[i]]:
+            s.process_images(H.cuda(d), H.cuda(c))
+            poses.append(s.get_camera_pose())
+        alone.append(poses)
+        s.close()
+
+    sess = [L.System(K, cfgs[i]) for i in range(n)]
+    batch = L.FusionBatch(n)
+    for i, s in enumerate(sess):
+        s.set_pose(fr[seeds[i]][0][2])
+        batch.set(i, s)
+    batch.set_groups(1)
+    for k in range(nf):
+        for i, s in enumerate(sess):
+            d, c, _ = fr[seeds[i]][k]
+            s.stage(H.cuda(d), H.cuda(c))
+        batch.process([True] * n, use_graph=True)
+        torch.cuda.synchronize()
+        for i, s in enumerate(sess):
+            assert np.array_equal(s.get_camera_pose(), alone[i][k]), (i, k)
+    batch.close()
+    for s in sess:
+        s.close()
+
 def test_batch_staging_pipeline_matches_session_staging(gbf):
     """Frames staged into the batch's double-buffered inputs on a copy stream,
     one tick ahead of the compute, and results read one tick behind give the
