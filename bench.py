@@ -17,6 +17,7 @@ sessions (replicas, no collective on the data path); rank 0 prints.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -435,10 +436,10 @@ def precision_check(L, K, cfg, fr, g, threads):
     om = O.OracleMap(oc, ok, "f64")
     for (d, c, T), n in zip(fr, g["nmaps"]):
         om.fuse(d.astype(np.float32) * np.float32(0.001), c, T, nmap=n)
-    gc, gs, gw, _ = g["map"]
+    gcoord, gs, gw, _ = g["map"]
     oc_, os_, ow, _ = om.export()
     key = lambda a: a[:, 0].astype(np.int64) * (1 << 42) + a[:, 1].astype(np.int64) * (1 << 21) + a[:, 2]
-    gk, okk = key(gc.astype(np.int64) + (1 << 20)), key(oc_.astype(np.int64) + (1 << 20))
+    gk, okk = key(gcoord.astype(np.int64) + (1 << 20)), key(oc_.astype(np.int64) + (1 << 20))
     common, gi, oi = np.intersect1d(gk, okk, return_indices=True)
     gs, gw, os_, ow = gs[gi], gw[gi], os_[oi], ow[oi]
     both = (gw > 0) & (ow > 0)
@@ -678,6 +679,10 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
+    # the timed loops run with Python's garbage collector paused (as timeit does):
+    # a collection pass in the host loop would stall the submission of ticks
+    gc.collect()
+    gc.disable()
     with ClockSampler(local) as clocks:
         clocks.start()
         t_wall = time.perf_counter()
@@ -688,6 +693,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
         clocks.stop()
+    gc.enable()
     if world > 1:
         dist.barrier()
     tick_ms = [a.elapsed_time(b) for a, b in ev]
@@ -787,6 +793,8 @@ def run_ours(args):
     eb.results(back=0)
     torch.cuda.synchronize()
     got.clear()
+    gc.collect()
+    gc.disable()
     with ClockSampler(local) as e2e_clocks:
         e2e_clocks.start()
         t_e2e = time.perf_counter()
@@ -795,6 +803,7 @@ def run_ours(args):
         got.append(eb.results(back=0))
         t_e2e = time.perf_counter() - t_e2e
         e2e_clocks.stop()
+    gc.enable()
     assert len(got) == n_e2e
     e2e = {"value": S * world * n_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": S * W * H * 5,
            "d2h_bytes_per_step": S * 144, "steps": n_e2e, "clocks": e2e_clocks.summary(),
@@ -1297,9 +1306,9 @@ def run_precision(args):
     ovtx, _ = om.mesh(0, 1 << 23)
     otree = cKDTree(ovtx.reshape(-1, 3).astype(np.float64))
     for name, m in maps.items():
-        gc, gs, gw, _ = m.export()
+        gcoord, gs, gw, _ = m.export()
         gi, oi = [], []
-        for i, x in enumerate(gc.tolist()):
+        for i, x in enumerate(gcoord.tolist()):
             j = okey.get(tuple(x))
             if j is not None:
                 gi.append(i)
