@@ -435,18 +435,20 @@ def test_raycast_maps_bit_exact(gbf, layout):
     assert np.array_equal(np.nan_to_num(vm2.cpu().numpy(), nan=7.0), np.nan_to_num(g, nan=7.0))
 
 
-def test_post_raycast_pyramid_bit_exact(gbf):
+@pytest.mark.parametrize("w,h", [(320, 240), (328, 248), (1280, 720)])
+def test_post_raycast_pyramid_bit_exact(gbf, w, h):
     """DeviceImage::resize_device_map (src/tracking/device_image.cpp:188-199):
     after a frame, the next frame's reference vertex map is the raycast at the
     tracked pose (level 0), levels 1-2 its 2x2 means, and every level's normals
     recomputed from it.  Level 0 is checked against a raycast of the same map
     at the same pose, levels 1-2 and all normal maps bit for bit against the
-    oracle's pyramid built from that level 0."""
+    oracle's pyramid built from that level 0; at 328x248 the 32x32 tiles of the
+    one-pass pyramid kernel end ragged on every level (328, 164, 82 wide)."""
     import oracle as O
     import torch
     L = gbf
-    K = H.intrinsics(L)
-    cfg = H.small_config(L, 0, bilateral=0)
+    K = H.intrinsics(L, w, h)
+    cfg = H.small_config(L, 0, bilateral=0, num_blocks=1 << 17, num_buckets=1 << 18)  # room for every block
     fr = H.frames(L, K, 3)
     s = L.System(K, cfg)
     s.set_pose(fr[0][2])
