@@ -150,6 +150,50 @@ def test_step_launch_of_a_large_batch_matches_sessions_alone(gbf):
     for s in sess:
         s.close()
 
+
+def test_pitched_staging_matches_dense_staging(gbf):
+    """Frames staged from pitched rows (a camera buffer wider than the image,
+    pinned host and device memory) give the same poses and map as the same
+    frames staged from dense rows: dense rows go as one contiguous copy, pitched
+    ones row by row."""
+    import ctypes as C
+    import torch
+    from libfusion_gb300 import call
+    L = gbf
+    K = H.intrinsics(L, 320, 240)
+    W, Hh = K.width, K.height
+    fr = H.frames(L, K, 4, seed=5)
+
+    def run(pitched, host):
+        s = L.System(K, H.small_config(L, 2))
+        s.set_pose(fr[0][2])
+        poses = []
+        for d, c, _ in fr:
+            if pitched:
+                dp = torch.zeros((Hh, W + 24), dtype=torch.uint16)
+                cp = torch.zeros((Hh, W * 3 + 40), dtype=torch.uint8)
+                dp[:, :W] = torch.from_numpy(d)
+                cp[:, :W * 3] = torch.from_numpy(np.ascontiguousarray(c).reshape(Hh, W * 3))
+            else:
+                dp, cp = torch.from_numpy(np.ascontiguousarray(d)), torch.from_numpy(np.ascontiguousarray(c))
+            dp = dp.pin_memory() if host else dp.cuda()
+            cp = cp.pin_memory() if host else cp.cuda()
+            call("gbf_session_stage", s._h, dp.data_ptr(), dp.stride(0) * 2, cp.data_ptr(),
+                 cp.stride(0) if pitched else W * 3, C.c_void_p(0))
+            s.process_staged()
+            poses.append(s.get_camera_pose())
+        torch.cuda.synchronize()
+        out = poses, s.export()
+        s.close()
+        return out
+
+    for host in (True, False):
+        pd, md = run(False, host)
+        pp, mp = run(True, host)
+        assert all(np.array_equal(a, b) for a, b in zip(pd, pp))
+        for x, y in zip(md, mp):  # blocks in coordinate order (ids follow insertion order)
+            assert np.array_equal(H.sort_blocks(md[0], x)[1], H.sort_blocks(mp[0], y)[1])
+
 def test_batch_staging_pipeline_matches_session_staging(gbf):
     """Frames staged into the batch's double-buffered inputs on a copy stream,
     one tick ahead of the compute, and results read one tick behind give the
