@@ -683,17 +683,19 @@ def run_ours(args):
     # a collection pass in the host loop would stall the submission of ticks
     gc.collect()
     gc.disable()
-    with ClockSampler(local) as clocks:
-        clocks.start()
-        t_wall = time.perf_counter()
-        for k in range(steps):
-            ev[k][0].record(stream)
-            tick(warm + k)
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
-        t_wall = time.perf_counter() - t_wall
-        clocks.stop()
-    gc.enable()
+    try:
+        with ClockSampler(local) as clocks:
+            clocks.start()
+            t_wall = time.perf_counter()
+            for k in range(steps):
+                ev[k][0].record(stream)
+                tick(warm + k)
+                ev[k][1].record(stream)
+            torch.cuda.synchronize()
+            t_wall = time.perf_counter() - t_wall
+            clocks.stop()
+    finally:
+        gc.enable()
     if world > 1:
         dist.barrier()
     tick_ms = [a.elapsed_time(b) for a, b in ev]
@@ -738,8 +740,9 @@ def run_ours(args):
                                  "times this run's pixel-iterations per launch" if traffic is not None else None,
                 "work_per_step": {"pixel_iterations": pix_iter, "integrated_blocks": (ib1 - ib0) / phases["ticks"]},
                 "timing": f"CUDA events around the phase over {phases['ticks']} ticks on the launching stream",
-                "why_this_kernel": "the raycast (39% of launch time against the reduction's 27% and its step's 4% in an ncu "
-                                   "launch list of the 64-session tick) is bound by instruction issue, not HBM "
+                "why_this_kernel": "the raycast (39% of launch time against the reduction's 27% and its step's "
+                                   "4% in an ncu launch list of the 64-session tick) is bound by instruction "
+                                   "issue, not HBM "
                                    "(74% issue active, DRAM 3.8% in its ncu capture at 4 sessions), so its "
                                    "figures are under 'march'; the HBM roofline is given for the memory-bound phase",
                 "march_ms_per_step": phases["march"]}
@@ -795,15 +798,17 @@ def run_ours(args):
     got.clear()
     gc.collect()
     gc.disable()
-    with ClockSampler(local) as e2e_clocks:
-        e2e_clocks.start()
-        t_e2e = time.perf_counter()
-        for k in range(warm, warm + n_e2e):
-            e2e_tick(k, warm)
-        got.append(eb.results(back=0))
-        t_e2e = time.perf_counter() - t_e2e
-        e2e_clocks.stop()
-    gc.enable()
+    try:
+        with ClockSampler(local) as e2e_clocks:
+            e2e_clocks.start()
+            t_e2e = time.perf_counter()
+            for k in range(warm, warm + n_e2e):
+                e2e_tick(k, warm)
+            got.append(eb.results(back=0))
+            t_e2e = time.perf_counter() - t_e2e
+            e2e_clocks.stop()
+    finally:
+        gc.enable()
     assert len(got) == n_e2e
     e2e = {"value": S * world * n_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": S * W * H * 5,
            "d2h_bytes_per_step": S * 144, "steps": n_e2e, "clocks": e2e_clocks.summary(),
